@@ -1,0 +1,390 @@
+#!/usr/bin/env python
+"""Benchmark of the FZ compression hot path on GB300.
+
+A step is one pass of the path over one batch of synthetic input: `--fields` (8)
+independent exafel-like 39200x388 float32 fields (the single-field workload the metric
+is quoted on; configs[1], relative eb 1e-3), each compressed (range pass + fused
+compress kernel) and then decompressed (decode + inverse Lorenzo) on the device.  The
+batch holds 8 x 60.8 MB = 486 MB of input, larger than the 129 MB L2, and every field
+is visited once per step, so each step reads its inputs from HBM.
+
+  value      uncompressed GB/s through the codec, both directions:
+             steps * fields * 2 * 4n bytes / device time (CUDA events), summed over ranks
+  e2e        the same metric through the host-buffer C-ABI calls fz_compress_host /
+             fz_decompress_host (pinned host memory, H2D and D2H copies inside the region)
+  roofline   the dominant kernel's algorithmic bytes per launch / its mean event-timed
+             launch duration, against the measured HBM copy bandwidth
+  cpu_baseline  the oracle (C, OpenMP) on this host's cores, round trips of one field
+
+`--impl reference` times the reference path's CPU restatement (the oracle port; the
+reference has no CPU implementation and its GPU code is not a CPU baseline) on the
+same metric and workload.  Under torchrun each rank runs its own batch (weak scaling);
+only rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIMS = (39200, 388, 1)
+EB = 1e-3
+WORKLOAD = "exafel-like 39200x388 f32 (peaks on N(0,0.5) background), relative eb 1e-3"
+METRIC = "compress/decompress GB/s + %HBM peak"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--fields", type=int, default=8)
+    p.add_argument("--impl", choices=["fz", "reference"], default="fz")
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    """Samples SM clock and clock-event reasons through NVML (read-only) every ~2 ms."""
+    REASONS = {0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_cap",
+               0x8: "hw_slowdown", 0x10: "sync_boost", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown",
+               0x100: "display_clock_setting"}
+
+    def __init__(self, device_index):
+        self.samples, self.reasons, self.max_mhz = [], 0, None
+        self.ok = False
+        try:
+            self.nv = C.CDLL("libnvidia-ml.so.1")
+            if self.nv.nvmlInit_v2() != 0:
+                return
+            self.h = C.c_void_p()
+            bus = self._bus_id(device_index)
+            rc = self.nv.nvmlDeviceGetHandleByPciBusId_v2(bus, C.byref(self.h)) if bus else 1
+            if rc != 0 and self.nv.nvmlDeviceGetHandleByIndex_v2(device_index, C.byref(self.h)) != 0:
+                return
+            m = C.c_uint()
+            if self.nv.nvmlDeviceGetMaxClockInfo(self.h, 1, C.byref(m)) == 0:
+                self.max_mhz = m.value
+            self.fn_reasons = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                getattr(self.nv, "nvmlDeviceGetCurrentClocksThrottleReasons")
+            self.ok = True
+        except OSError:
+            pass
+
+    @staticmethod
+    def _bus_id(dev):
+        try:
+            rt = C.CDLL("libcudart.so")
+        except OSError:
+            try:
+                import torch  # noqa: F401  (torch's cudart is already loaded)
+                rt = C.CDLL(None)
+            except OSError:
+                return None
+        buf = C.create_string_buffer(64)
+        try:
+            if rt.cudaDeviceGetPCIBusId(buf, 64, dev) == 0:
+                return buf.value
+        except AttributeError:
+            return None
+        return None
+
+    def _run(self):
+        mhz, r = C.c_uint(), C.c_ulonglong()
+        while not self._stop.is_set():
+            if self.nv.nvmlDeviceGetClockInfo(self.h, 1, C.byref(mhz)) == 0:
+                self.samples.append(mhz.value)
+            if self.fn_reasons(self.h, C.byref(r)) == 0:
+                self.reasons |= r.value
+            time.sleep(0.002)
+
+    def __enter__(self):
+        if self.ok:
+            self._stop = threading.Event()
+            self._t = threading.Thread(target=self._run, daemon=True)
+            self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        if self.ok:
+            self._stop.set()
+            self._t.join()
+
+    def summary(self):
+        if not self.ok:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvml unavailable"], "samples": 0}
+        names = [v for k, v in self.REASONS.items() if self.reasons & k and k != 0x1]
+        return {"sm_mhz": statistics.median(self.samples) if self.samples else None,
+                "sm_max_mhz": self.max_mhz, "reasons": names, "samples": len(self.samples)}
+
+
+# --------------------------------------------------------------- workload --
+def make_fields(count, seed0):
+    import importlib
+    import __graft_entry__ as g
+    g.load_package()
+    synth = importlib.import_module("fz_gpu_gb300.synth")
+    return [synth.peaks2d(DIMS[0], DIMS[1], seed=seed0 + i) for i in range(count)]
+
+
+def cpu_round_trips(field, seconds, min_reps=2):
+    """Oracle round trips of one field until `seconds` of CPU work; returns (GB/s, reps, s)."""
+    import oracle
+    n = field.size
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        st = oracle.compress(field, DIMS, EB, rel=True, mode=1)
+        oracle.decompress(st)
+        reps += 1
+        el = time.perf_counter() - t0
+        if (el >= seconds and reps >= min_reps) or el > 3 * seconds:
+            break
+    return 2 * 4 * n * reps / el / 1e9, reps, el
+
+
+def run_reference(args, rank, world):
+    """The reference path's CPU restatement on this host (rank 0 only)."""
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    field = make_fields(1, 1)[0]
+    n = field.size
+    for _ in range(args.warmup):
+        oracle.decompress(oracle.compress(field, DIMS, EB, rel=True, mode=1))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = oracle.compress(field, DIMS, EB, rel=True, mode=1)
+        oracle.decompress(st)
+    el = time.perf_counter() - t0
+    gbs = 2 * 4 * n * args.steps / el / 1e9
+    line = {
+        "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * el / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": WORKLOAD + ", one field per step (compress + decompress)",
+                   "field_elems": n},
+        "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": oracle.threads(), "kind": "port",
+                         "sample": f"{args.steps} round trips of one {DIMS[0]}x{DIMS[1]} field"},
+        "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_fz(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import __graft_entry__ as g
+
+    fz = g.load_package()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    L = fz.lib()
+    fields = make_fields(args.fields, 1 + rank * args.fields)
+    n = fields[0].size
+    cap = fz.max_compressed_bytes(n, DIMS, fz.MODE_SIDECAR)
+    X = [torch.from_numpy(f).to(dev) for f in fields]
+    S = [torch.empty(cap, dtype=torch.uint8, device=dev) for _ in fields]
+    Y = [torch.empty(n, dtype=torch.float32, device=dev) for _ in fields]
+    ws = fz.Workspace(n)
+    stream = torch.cuda.current_stream(dev)
+    sh = C.c_void_p(stream.cuda_stream)
+    dims = fz._dims(DIMS)
+
+    # first pass: validate and keep each field's header (decompression takes it from
+    # the host, as a caller that just compressed would)
+    headers, sizes = [], []
+    for i in range(args.fields):
+        nb = C.c_uint64()
+        fz._check("compress", L.fz_compress(ws.handle, C.c_void_p(X[i].data_ptr()), n, dims, EB, fz.EB_REL,
+                                            fz.MODE_SIDECAR, C.c_void_p(S[i].data_ptr()), cap, C.byref(nb), sh))
+        h = fz.parse_header(S[i][:64].cpu().numpy())
+        headers.append(h)
+        sizes.append(nb.value)
+    args_c = [(C.c_void_p(X[i].data_ptr()), C.c_void_p(S[i].data_ptr()), C.c_void_p(Y[i].data_ptr()),
+               C.byref(headers[i]), sizes[i]) for i in range(args.fields)]
+
+    def step():
+        for xp, sp, yp, hp, sb in args_c:
+            st = L.fz_compress(ws.handle, xp, n, dims, EB, fz.EB_REL, fz.MODE_SIDECAR, sp, cap, None, sh)
+            st |= L.fz_decompress(ws.handle, sp, sb, hp, yp, n, sh)
+            if st:
+                raise fz.FzError("bench step", st)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # spot check: the reconstruction of the last field meets the error bound
+    err = (Y[-1] - X[-1]).abs().max().item()
+    assert err <= headers[-1].eb_abs * (1 + 2 ** -10) + 1e-6 * X[-1].abs().max().item(), err
+
+    ws.enable_timing(args.steps * args.fields * 4 + 16)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local_rank)
+    with clocks:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = t.item()
+    kern = {}
+    launches = 0
+    for k in fz.Workspace.KERNELS:
+        cnt, tot = ws.kernel_time(k)
+        kern[k] = (cnt, tot)
+        launches += cnt
+    ws.enable_timing(0)
+
+    bytes_step = args.fields * 2 * 4 * n
+    value = bytes_step * args.steps * world / (ms / 1e3) / 1e9
+    hbm, src = peaks()
+    stream_b = float(np.mean(sizes))
+    algo = {"k_range": 4 * n, "k_compress": 4 * n + stream_b, "k_decode": stream_b + 2 * n,
+            "k_recon": 2 * n + 4 * n}
+    kernels = {}
+    for k, (cnt, tot) in kern.items():
+        if cnt:
+            us = 1e3 * tot / cnt
+            gbs = algo[k] / (us * 1e-6) / 1e9
+            kernels[k] = {"launches": cnt, "mean_us": round(us, 3), "algo_bytes": int(algo[k]),
+                          "achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm, 4),
+                          "share": round(tot / sum(v[1] for v in kern.values()), 4)}
+    dom = max(kernels, key=lambda k: kernels[k]["launches"] * kernels[k]["mean_us"])
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(dom, {}).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    t_c = sum(kern[k][1] for k in ("k_range", "k_compress")) / max(1, kern["k_compress"][0])
+    t_d = sum(kern[k][1] for k in ("k_decode", "k_recon")) / max(1, kern["k_decode"][0])
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator standing in for the EXAFEL field, no dataset)",
+        "config": {"workload": WORKLOAD, "fields_per_step": args.fields, "field_elems": n,
+                   "mode": "sidecar", "stream_bytes_mean": int(stream_b),
+                   "ratio_reference_formula": round(fz.reference_sizes(4 * n, headers[0].nnz)[2], 4),
+                   "l2": f"inputs {args.fields * 4 * n / 1e6:.0f} MB per step > 129 MB L2; each field visited once per step"},
+        "compress_gbs": round(4 * n / (t_c * 1e-3) / 1e9, 1),
+        "decompress_gbs": round(4 * n / (t_d * 1e-3) / 1e9, 1),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": kernels[dom]["achieved_gbs"], "peak": hbm,
+                     "peak_source": src, "unit": "GB/s", "frac": kernels[dom]["frac"],
+                     "traffic": traffic, "algo_bytes": kernels[dom]["algo_bytes"]},
+        "kernels": kernels,
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    if not args.no_e2e:
+        line["e2e"] = e2e(fz, L, fields, n, cap, sizes, args, dev, world, dist)
+    if rank == 0 and world == 1:
+        import oracle
+        oracle.build()
+        gbs, reps, el = cpu_round_trips(fields[0], args.cpu_seconds)
+        line["cpu_baseline"] = {"value": round(gbs, 3), "unit": "GB/s", "cores": oracle.threads(),
+                                "kind": "port", "sample": f"{reps} round trips of one {DIMS[0]}x{DIMS[1]} field ({el:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def e2e(fz, L, fields, n, cap, sizes, args, dev, world, dist):
+    """Host-buffer round trips through fz_compress_host / fz_decompress_host."""
+    import numpy as np
+    import torch
+    steps = min(args.steps, 30)
+    hin = [torch.from_numpy(f).pin_memory() for f in fields]
+    hst = torch.empty(cap, dtype=torch.uint8).pin_memory()
+    hout = torch.empty(n, dtype=torch.float32).pin_memory()
+    ws = fz.Workspace(n)
+    dims = fz._dims(DIMS)
+    sh = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+    def one(i):
+        nb = C.c_uint64()
+        st = L.fz_compress_host(ws.handle, C.c_void_p(hin[i].data_ptr()), n, dims, EB, fz.EB_REL,
+                                fz.MODE_SIDECAR, C.c_void_p(hst.data_ptr()), cap, C.byref(nb), sh)
+        st |= L.fz_decompress_host(ws.handle, C.c_void_p(hst.data_ptr()), nb.value,
+                                   C.c_void_p(hout.data_ptr()), n, sh)
+        if st:
+            raise fz.FzError("e2e", st)
+        return nb.value
+
+    for i in range(min(3, len(fields))):
+        one(i)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    total_stream = 0
+    for _ in range(steps):
+        for i in range(len(fields)):
+            total_stream += one(i)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([el], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        el = t.item()
+    last = fields[(steps * len(fields) - 1) % len(fields)]
+    err = float(np.max(np.abs(hout.numpy().astype(np.float64) - last)))
+    assert err <= 1e-3 * float(np.float32(last.max() - last.min())) * 1.001, err
+    per_step_stream = total_stream / steps
+    return {"value": round(len(fields) * 2 * 4 * n * steps * world / el / 1e9, 2), "unit": "GB/s",
+            "steps": steps, "h2d_bytes_per_step": int(len(fields) * 4 * n + per_step_stream),
+            "d2h_bytes_per_step": int(per_step_stream + len(fields) * 4 * n)}
+
+
+def main():
+    args = parse_args()
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_fz(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

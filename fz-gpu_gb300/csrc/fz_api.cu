@@ -1,0 +1,611 @@
+// fz_api.cu -- the C ABI (include/fz.h): argument checks, stream layout, workspace,
+// and the launch sequences of the full pipeline and of the stage-level drop-ins.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/fz.h"
+#include "fz_internal.h"
+
+using namespace fz;
+
+namespace fz {
+
+Layout make_layout(uint64_t n, uint32_t x, uint32_t y, uint32_t z, uint32_t mode)
+{
+    Layout L{};
+    L.n      = (uint32_t)n;
+    L.x      = x, L.y = y, L.z = z;
+    L.xy     = x * y;
+    L.nl     = x * y * z;
+    L.ndim   = (z == 1 && y == 1) ? 1 : (z == 1 ? 2 : 3);
+    L.nb     = (uint32_t)(n / kBlockCodes);
+    L.tail   = (uint32_t)(n - (uint64_t)L.nb * kBlockCodes);
+    L.nwords = (uint32_t)cdiv(n, 256);
+    L.mode   = mode;
+    L.off_a  = kHeaderBytes;
+    L.off_c  = L.off_a + pad16(4ull * L.nwords);
+    uint64_t sc = 0;
+    if (mode == FZ_MODE_SIDECAR) {
+        sc += pad16(2ull * L.tail);
+        L.off_sign = L.off_c + sc;
+        if (L.ndim == 1) sc += pad16(4 * cdiv(n, 32));
+    } else {
+        L.off_sign = L.off_c;
+    }
+    L.sidecar_bytes = (uint32_t)sc;
+    L.off_b         = L.off_c + sc;
+    return L;
+}
+
+}  // namespace fz
+
+struct fz_workspace {
+    int       device;
+    uint64_t  max_n;
+    uint32_t  max_tiles;
+    void*     d_base;
+    size_t    d_bytes;
+    uint64_t* state;
+    uint32_t* tickets;  // [0] compress, [1] decode, [2] scan-encode, [3] range
+    uint32_t* status;
+    uint32_t* total;
+    float2*   partials;
+    EbInfo*   eb;
+    uint16_t* codes;
+    uint32_t  epoch;
+    uint8_t*  h_pinned;  // 64-byte header + status word
+    // host-buffer path staging, allocated on first use
+    float*    d_field;
+    uint8_t*  d_stream;
+    uint64_t  stream_cap;
+    // per-kernel timing ring (fz_workspace_enable_timing)
+    std::vector<cudaEvent_t> tev;   // 2 per record
+    std::vector<int>         tkind;
+    uint32_t                 tcap  = 0;
+    uint32_t                 tused = 0;
+};
+
+namespace {
+
+constexpr uint64_t kMaxN = 1ull << 31;
+
+fz_status map_err(cudaError_t e, fz_status dflt = FZ_FAIL_GPU_ILLEGAL_ACCESS)
+{
+    if (e == cudaSuccess) return FZ_SUCCESS;
+    if (e == cudaErrorMemoryAllocation) return FZ_FAIL_GPU_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return FZ_NO_DEVICE;
+    return dflt;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+int ndim_of(fz_dims d) { return (d.z == 1 && d.y == 1) ? 1 : (d.z == 1 ? 2 : 3); }
+
+fz_status check_dims(uint64_t n, fz_dims d)
+{
+    if (n == 0 || n > kMaxN || d.x == 0 || d.y == 0 || d.z == 0) return FZ_INVALID_ARG;
+    const uint64_t nl = (uint64_t)d.x * d.y * d.z;
+    if (nl > n) return FZ_INVALID_ARG;
+    return FZ_SUCCESS;
+}
+
+uint64_t max_stream(const Layout& L) { return L.off_b + 16ull * kChunks * L.nb; }
+
+uint32_t next_epoch(fz_workspace* ws, cudaStream_t s)
+{
+    ws->epoch++;
+    if (ws->epoch >= (1u << 28)) {
+        // the 28-bit epoch tag wraps: clear the tile states once
+        cudaMemsetAsync(ws->state, 0, (size_t)ws->max_tiles * 8, s);
+        ws->epoch = 1;
+    }
+    return ws->epoch;
+}
+
+// Brackets one kernel launch with a pair of events when timing is enabled.
+struct KernelTimer {
+    fz_workspace* ws;
+    cudaStream_t  s;
+    int           kind;
+    bool          on;
+    KernelTimer(fz_workspace* w, cudaStream_t st, int k) : ws(w), s(st), kind(k)
+    {
+        on = ws->tcap && ws->tused < ws->tcap;
+        if (on) cudaEventRecord(ws->tev[2 * ws->tused], s);
+    }
+    ~KernelTimer()
+    {
+        if (!on) return;
+        cudaEventRecord(ws->tev[2 * ws->tused + 1], s);
+        ws->tkind[ws->tused++] = kind;
+    }
+};
+
+fz_status check_device(const fz_workspace* ws)
+{
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FZ_NO_DEVICE;
+    return dev == ws->device ? FZ_SUCCESS : FZ_INVALID_ARG;
+}
+
+// Reads back the header and the sticky status word (syncs), clears the status.
+fz_status readback(fz_workspace* ws, const void* d_stream, cudaStream_t s, fz_header* h)
+{
+    cudaError_t e = cudaMemcpyAsync(ws->h_pinned, d_stream, 64, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ws->h_pinned + 64, ws->status, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return map_err(e, FZ_FAIL_GPU_MEMCPY);
+    std::memcpy(h, ws->h_pinned, 64);
+    uint32_t st;
+    std::memcpy(&st, ws->h_pinned + 64, 4);
+    if (st) cudaMemsetAsync(ws->status, 0, 4, s);
+    if (st & kStatusTimeout) return FZ_TIMEOUT;
+    if (st & kStatusNonfinite) return FZ_NONFINITE_INPUT;
+    if (st & kStatusCorrupt) return FZ_CORRUPT_STREAM;
+    return FZ_SUCCESS;
+}
+
+fz_status validate_header(const fz_header* h, uint64_t stream_bytes, Layout* out)
+{
+    if (h->magic != FZ_MAGIC || h->version != FZ_FORMAT_VERSION) return FZ_CORRUPT_STREAM;
+    if (h->mode > 1) return FZ_CORRUPT_STREAM;
+    fz_dims d{h->x, h->y, h->z};
+    if (check_dims(h->n, d) != FZ_SUCCESS || ndim_of(d) != h->ndim) return FZ_CORRUPT_STREAM;
+    Layout L = make_layout(h->n, h->x, h->y, h->z, h->mode);
+    if (L.sidecar_bytes != h->sidecar_bytes) return FZ_CORRUPT_STREAM;
+    if (h->nnz > (uint64_t)L.nb * kChunks) return FZ_CORRUPT_STREAM;
+    if (L.off_b + 16ull * h->nnz > stream_bytes) return FZ_CORRUPT_STREAM;
+    *out = L;
+    return FZ_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fz_status_string(fz_status s)
+{
+    switch (s) {
+    case FZ_SUCCESS: return "success";
+    case FZ_FAIL_ONDISK_FILE_ERROR: return "file error";
+    case FZ_FAIL_DATA_NOT_READY: return "data not ready";
+    case FZ_FAIL_GPU_MALLOC: return "device allocation failed";
+    case FZ_FAIL_GPU_MEMCPY: return "device copy failed";
+    case FZ_FAIL_GPU_ILLEGAL_ACCESS: return "device launch or execution failed";
+    case FZ_FAIL_GPU_OUT_OF_MEMORY: return "device out of memory";
+    case FZ_FAIL_INCOMPRESSIABLE: return "incompressible";
+    case FZ_FAIL_UNSUPPORTED_DATATYPE: return "unsupported data type";
+    case FZ_NOT_IMPLEMENTED: return "not implemented";
+    case FZ_INVALID_ARG: return "invalid argument";
+    case FZ_CORRUPT_STREAM: return "corrupt stream";
+    case FZ_OUT_OF_SPACE: return "output buffer too small";
+    case FZ_TIMEOUT: return "device-side wait timed out";
+    case FZ_NO_DEVICE: return "no CUDA device";
+    case FZ_NONFINITE_INPUT: return "non-finite input with a relative error bound";
+    }
+    return "unknown status";
+}
+
+const char* fz_version(void) { return "fz-gb300 1.0 (sm_103a)"; }
+
+int fz_ndim(fz_dims dims) { return ndim_of(dims); }
+
+fz_status fz_stream_layout(uint64_t n, fz_dims dims, fz_mode mode, uint64_t* off_a,
+                           uint64_t* off_c, uint64_t* off_b, uint32_t* sidecar_bytes)
+{
+    if (check_dims(n, dims) != FZ_SUCCESS || (mode != FZ_MODE_COMPAT && mode != FZ_MODE_SIDECAR))
+        return FZ_INVALID_ARG;
+    Layout L = make_layout(n, dims.x, dims.y, dims.z, mode);
+    if (off_a) *off_a = L.off_a;
+    if (off_c) *off_c = L.off_c;
+    if (off_b) *off_b = L.off_b;
+    if (sidecar_bytes) *sidecar_bytes = L.sidecar_bytes;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_max_compressed_bytes(uint64_t n, fz_dims dims, fz_mode mode, uint64_t* bytes)
+{
+    if (!bytes || check_dims(n, dims) != FZ_SUCCESS || (mode != FZ_MODE_COMPAT && mode != FZ_MODE_SIDECAR))
+        return FZ_INVALID_ARG;
+    *bytes = max_stream(make_layout(n, dims.x, dims.y, dims.z, mode));
+    return FZ_SUCCESS;
+}
+
+fz_status fz_stream_bytes(const fz_header* h, uint64_t* bytes)
+{
+    if (!h || !bytes) return FZ_INVALID_ARG;
+    Layout    L;
+    fz_status st = validate_header(h, ~0ull, &L);
+    if (st != FZ_SUCCESS) return st;
+    *bytes = L.off_b + 16ull * h->nnz;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_reference_sizes(uint64_t file_bytes, uint64_t nnz, uint64_t* original,
+                             uint64_t* compressed, double* ratio)
+{
+    // fz.cu:118 len = fileSize/4; :178 dataChunkSize = ceil(2 len / 512); :208-209
+    const uint64_t len = file_bytes / 4;
+    const uint64_t dcs = cdiv(2 * len, 512);
+    const uint64_t c   = 4 * dcs + 16 * nnz;
+    if (original) *original = file_bytes;
+    if (compressed) *compressed = c;
+    if (ratio) *ratio = c ? (double)((float)file_bytes / (float)c) : 0.0;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_workspace_bytes(uint64_t max_n, uint64_t* bytes)
+{
+    if (!bytes || max_n == 0 || max_n > kMaxN) return FZ_INVALID_ARG;
+    const uint64_t tiles = max_n / kBlockCodes + 2;
+    uint64_t       b     = 0;
+    b += pad16(8 * tiles);          // state
+    b += 64;                        // tickets, status, total
+    b += pad16(8 * kRangeGrid);     // partials
+    b += pad16(sizeof(EbInfo));     // eb
+    b += pad16(2 * max_n + 16);     // decode scratch
+    *bytes = b;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_workspace_create(uint64_t max_n, fz_workspace** out)
+{
+    if (!out) return FZ_INVALID_ARG;
+    *out = nullptr;
+    uint64_t bytes;
+    if (fz_workspace_bytes(max_n, &bytes) != FZ_SUCCESS) return FZ_INVALID_ARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FZ_NO_DEVICE;
+    fz_workspace* ws = new (std::nothrow) fz_workspace();
+    if (!ws) return FZ_FAIL_GPU_MALLOC;
+    ws->device    = dev;
+    ws->max_n     = max_n;
+    ws->max_tiles = (uint32_t)(max_n / kBlockCodes + 2);
+    cudaError_t e = cudaMalloc(&ws->d_base, bytes);
+    if (e != cudaSuccess) {
+        delete ws;
+        return map_err(e, FZ_FAIL_GPU_MALLOC);
+    }
+    ws->d_bytes = bytes;
+    uint8_t* p  = static_cast<uint8_t*>(ws->d_base);
+    ws->state   = reinterpret_cast<uint64_t*>(p), p += pad16(8ull * ws->max_tiles);
+    ws->tickets = reinterpret_cast<uint32_t*>(p);
+    ws->status  = ws->tickets + 4;
+    ws->total   = ws->tickets + 5;
+    p += 64;
+    ws->partials = reinterpret_cast<float2*>(p), p += pad16(8 * kRangeGrid);
+    ws->eb       = reinterpret_cast<EbInfo*>(p), p += pad16(sizeof(EbInfo));
+    ws->codes    = reinterpret_cast<uint16_t*>(p);
+    e            = cudaMemset(ws->d_base, 0, bytes);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&ws->h_pinned, 128);
+    if (e != cudaSuccess) {
+        cudaFree(ws->d_base);
+        delete ws;
+        return map_err(e, FZ_FAIL_GPU_MALLOC);
+    }
+    ws->epoch = 0;
+    *out      = ws;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_workspace_enable_timing(fz_workspace* ws, uint32_t capacity)
+{
+    if (!ws) return FZ_INVALID_ARG;
+    for (cudaEvent_t e : ws->tev) cudaEventDestroy(e);
+    ws->tev.assign(2 * (size_t)capacity, nullptr);
+    ws->tkind.assign(capacity, -1);
+    ws->tused = 0;
+    ws->tcap  = 0;
+    for (auto& e : ws->tev) {
+        cudaError_t r = cudaEventCreate(&e);
+        if (r != cudaSuccess) return map_err(r);
+    }
+    ws->tcap = capacity;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_workspace_kernel_time(fz_workspace* ws, int kind, uint32_t* launches, double* total_ms)
+{
+    if (!ws || !launches || !total_ms) return FZ_INVALID_ARG;
+    *launches = 0;
+    *total_ms = 0;
+    if (ws->tused) {
+        cudaError_t r = cudaEventSynchronize(ws->tev[2 * ws->tused - 1]);
+        if (r != cudaSuccess) return map_err(r);
+    }
+    uint32_t keep = 0;
+    for (uint32_t i = 0; i < ws->tused; ++i) {
+        if (ws->tkind[i] == kind) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ws->tev[2 * i], ws->tev[2 * i + 1]);
+            *total_ms += ms;
+            ++*launches;
+        } else {
+            // keep the other kinds' records, compacted to the front
+            std::swap(ws->tev[2 * keep], ws->tev[2 * i]);
+            std::swap(ws->tev[2 * keep + 1], ws->tev[2 * i + 1]);
+            ws->tkind[keep++] = ws->tkind[i];
+        }
+    }
+    ws->tused = keep;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_workspace_destroy(fz_workspace* ws)
+{
+    if (!ws) return FZ_INVALID_ARG;
+    for (cudaEvent_t e : ws->tev) cudaEventDestroy(e);
+    cudaFree(ws->d_base);
+    cudaFreeHost(ws->h_pinned);
+    cudaFree(ws->d_field);
+    cudaFree(ws->d_stream);
+    delete ws;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_workspace_status(fz_workspace* ws, fz_stream_t stream)
+{
+    if (!ws) return FZ_INVALID_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t  e = cudaMemcpyAsync(ws->h_pinned + 64, ws->status, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return map_err(e, FZ_FAIL_GPU_MEMCPY);
+    uint32_t st;
+    std::memcpy(&st, ws->h_pinned + 64, 4);
+    if (st) cudaMemsetAsync(ws->status, 0, 4, s);
+    if (st & kStatusTimeout) return FZ_TIMEOUT;
+    if (st & kStatusNonfinite) return FZ_NONFINITE_INPUT;
+    if (st & kStatusCorrupt) return FZ_CORRUPT_STREAM;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_compress(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims dims, double eb,
+                      fz_eb_mode eb_mode, fz_mode mode, void* d_out, uint64_t out_capacity,
+                      uint64_t* out_bytes, fz_stream_t stream)
+{
+    if (!ws || !d_in || !d_out || !aligned16(d_in) || !aligned16(d_out)) return FZ_INVALID_ARG;
+    if (check_dims(n, dims) != FZ_SUCCESS || n > ws->max_n) return FZ_INVALID_ARG;
+    if (!(eb > 0) || !std::isfinite(eb)) return FZ_INVALID_ARG;
+    if ((eb_mode != FZ_EB_ABS && eb_mode != FZ_EB_REL) || (mode != FZ_MODE_COMPAT && mode != FZ_MODE_SIDECAR))
+        return FZ_INVALID_ARG;
+    fz_status st = check_device(ws);
+    if (st != FZ_SUCCESS) return st;
+    const Layout L = make_layout(n, dims.x, dims.y, dims.z, mode);
+    if (out_capacity < max_stream(L)) return FZ_OUT_OF_SPACE;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+
+    CompressArgs a{};
+    a.in = d_in, a.out = static_cast<uint8_t*>(d_out);
+    a.n = L.n, a.nl = L.nl, a.x = L.x, a.y = L.y, a.z = L.z, a.xy = L.xy;
+    a.dx = make_fastdiv(L.x), a.dxy = make_fastdiv(L.xy);
+    a.al_x = (L.x % 4) == 0, a.al_xy = (L.xy % 4) == 0, a.al_xyx = ((L.xy + L.x) % 4) == 0;
+    a.nb = L.nb, a.ntiles = L.nb + (L.tail ? 1 : 0), a.nwords = L.nwords;
+    a.mode = mode, a.ndim = L.ndim, a.sidecar_bytes = L.sidecar_bytes;
+    a.off_a = L.off_a, a.off_c = L.off_c, a.off_b = L.off_b, a.off_sign = L.off_sign;
+    a.state = ws->state, a.ticket = ws->tickets + 0, a.status = ws->status;
+    a.epoch = next_epoch(ws, s);
+    cudaError_t e = cudaSuccess;
+    if (eb_mode == FZ_EB_REL) {
+        KernelTimer t(ws, s, 0);
+        e    = launch_range(d_in, L.n, eb, 1, ws->partials, ws->tickets + 3, ws->eb, ws->status, s);
+        a.eb = ws->eb;
+    } else {
+        a.eb            = nullptr;
+        a.ebh.eb_abs    = eb;
+        const double e2 = eb * 2;  // lorenzo_var.cuh:562-563
+        a.ebh.ebx2_r    = (float)(1 / e2);
+        a.ebh.ebx2      = (float)e2;
+        a.ebh.range = a.ebh.vmin = a.ebh.vmax = 0.0f;
+    }
+    if (e == cudaSuccess) {
+        KernelTimer t(ws, s, 1);
+        e = launch_compress(a, s);
+    }
+    if (e != cudaSuccess) return map_err(e);
+    if (out_bytes) {
+        fz_header h;
+        st = readback(ws, d_out, s, &h);
+        *out_bytes = L.off_b + 16ull * h.nnz;
+        return st;
+    }
+    return FZ_SUCCESS;
+}
+
+fz_status fz_decompress(fz_workspace* ws, const void* d_stream, uint64_t stream_bytes,
+                        const fz_header* h_header, float* d_out, uint64_t out_capacity_elems,
+                        fz_stream_t stream)
+{
+    if (!ws || !d_stream || !d_out || !aligned16(d_stream) || !aligned16(d_out)) return FZ_INVALID_ARG;
+    if (stream_bytes < FZ_HEADER_BYTES) return FZ_CORRUPT_STREAM;
+    fz_status st = check_device(ws);
+    if (st != FZ_SUCCESS) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    fz_header    h;
+    if (h_header) {
+        h = *h_header;
+    } else {
+        cudaError_t e = cudaMemcpyAsync(ws->h_pinned, d_stream, 64, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return map_err(e, FZ_FAIL_GPU_MEMCPY);
+        std::memcpy(&h, ws->h_pinned, 64);
+    }
+    Layout L;
+    st = validate_header(&h, stream_bytes, &L);
+    if (st != FZ_SUCCESS) return st;
+    if (h.n > out_capacity_elems || h.n > ws->max_n) return FZ_OUT_OF_SPACE;
+
+    DecodeArgs d{};
+    d.st = static_cast<const uint8_t*>(d_stream);
+    d.codes = ws->codes;
+    d.n = L.n, d.nb = L.nb, d.tail = L.tail, d.mode = L.mode;
+    d.off_a = L.off_a, d.off_c = L.off_c, d.off_b = L.off_b, d.nnz = h.nnz;
+    d.state = ws->state, d.ticket = ws->tickets + 1, d.status = ws->status;
+    d.epoch = next_epoch(ws, s);
+    cudaError_t e;
+    {
+        KernelTimer t(ws, s, 2);
+        e = launch_decode(d, s);
+    }
+    if (e != cudaSuccess) return map_err(e);
+    ReconArgs r{};
+    r.codes    = ws->codes;
+    r.signbits = (L.ndim == 1 && L.mode == FZ_MODE_SIDECAR)
+                     ? reinterpret_cast<const uint32_t*>(d.st + L.off_sign) : nullptr;
+    r.signum = nullptr;
+    r.out    = d_out;
+    r.n = L.n, r.nl = L.nl, r.x = L.x, r.y = L.y, r.z = L.z;
+    r.ebx2 = h.ebx2;
+    {
+        KernelTimer t(ws, s, 3);
+        e = launch_reconstruct(r, s);
+    }
+    return map_err(e);
+}
+
+static fz_status ensure_staging(fz_workspace* ws, uint64_t n, uint64_t stream_bytes)
+{
+    if (!ws->d_field) {
+        cudaError_t e = cudaMalloc((void**)&ws->d_field, 4 * ws->max_n + 16);
+        if (e != cudaSuccess) return map_err(e, FZ_FAIL_GPU_MALLOC);
+    }
+    if (ws->stream_cap < stream_bytes) {
+        cudaFree(ws->d_stream);
+        ws->d_stream   = nullptr;
+        ws->stream_cap = 0;
+        // room for the largest stream of a max_n field (1D sidecar is the largest)
+        uint64_t cap = 0;
+        fz_dims  d1{(uint32_t)ws->max_n, 1, 1};
+        fz_max_compressed_bytes(ws->max_n, d1, FZ_MODE_SIDECAR, &cap);
+        if (cap < stream_bytes) cap = stream_bytes;
+        cudaError_t e = cudaMalloc((void**)&ws->d_stream, cap);
+        if (e != cudaSuccess) return map_err(e, FZ_FAIL_GPU_MALLOC);
+        ws->stream_cap = cap;
+    }
+    (void)n;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_compress_host(fz_workspace* ws, const float* h_in, uint64_t n, fz_dims dims,
+                           double eb, fz_eb_mode eb_mode, fz_mode mode, void* h_out,
+                           uint64_t out_capacity, uint64_t* out_bytes, fz_stream_t stream)
+{
+    if (!ws || !h_in || !h_out) return FZ_INVALID_ARG;
+    if (check_dims(n, dims) != FZ_SUCCESS || n > ws->max_n) return FZ_INVALID_ARG;
+    if (mode != FZ_MODE_COMPAT && mode != FZ_MODE_SIDECAR) return FZ_INVALID_ARG;
+    const Layout L = make_layout(n, dims.x, dims.y, dims.z, mode);
+    fz_status    st = ensure_staging(ws, n, max_stream(L));
+    if (st != FZ_SUCCESS) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t  e = cudaMemcpyAsync(ws->d_field, h_in, 4 * n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return map_err(e, FZ_FAIL_GPU_MEMCPY);
+    uint64_t bytes = 0;
+    st = fz_compress(ws, ws->d_field, n, dims, eb, eb_mode, mode, ws->d_stream, ws->stream_cap, &bytes, stream);
+    if (st != FZ_SUCCESS) return st;
+    if (bytes > out_capacity) return FZ_OUT_OF_SPACE;
+    e = cudaMemcpyAsync(h_out, ws->d_stream, bytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return map_err(e, FZ_FAIL_GPU_MEMCPY);
+    if (out_bytes) *out_bytes = bytes;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_decompress_host(fz_workspace* ws, const void* h_stream, uint64_t stream_bytes,
+                             float* h_out, uint64_t out_capacity_elems, fz_stream_t stream)
+{
+    if (!ws || !h_stream || !h_out || stream_bytes < FZ_HEADER_BYTES) return FZ_INVALID_ARG;
+    fz_header h;
+    std::memcpy(&h, h_stream, sizeof(h));
+    Layout    L;
+    fz_status st = validate_header(&h, stream_bytes, &L);
+    if (st != FZ_SUCCESS) return st;
+    if (h.n > out_capacity_elems || h.n > ws->max_n) return FZ_OUT_OF_SPACE;
+    st = ensure_staging(ws, h.n, stream_bytes);
+    if (st != FZ_SUCCESS) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t  e = cudaMemcpyAsync(ws->d_stream, h_stream, stream_bytes, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return map_err(e, FZ_FAIL_GPU_MEMCPY);
+    st = fz_decompress(ws, ws->d_stream, stream_bytes, &h, ws->d_field, ws->max_n, stream);
+    if (st != FZ_SUCCESS) return st;
+    e = cudaMemcpyAsync(h_out, ws->d_field, 4 * h.n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return map_err(e, FZ_FAIL_GPU_MEMCPY);
+    return fz_workspace_status(ws, stream);
+}
+
+fz_status fz_selftest_wait_timeout(fz_workspace* ws, fz_stream_t stream)
+{
+    if (!ws) return FZ_INVALID_ARG;
+    fz_status st = check_device(ws);
+    if (st != FZ_SUCCESS) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    // a fresh epoch: tile 0 holds a word of an older epoch, which reads as "not ready"
+    const uint32_t e = next_epoch(ws, s);
+    cudaError_t    r = launch_wait_selftest(ws->state, e, ws->status, s);
+    if (r != cudaSuccess) return map_err(r);
+    return fz_workspace_status(ws, stream);
+}
+
+// ------------------------------------------------------------------ stages --
+fz_status fz_lorenzo_construct(const float* d_data, uint16_t* d_quant, uint8_t* d_signum,
+                               fz_dims len3, double eb_abs, fz_stream_t stream)
+{
+    if (!d_data || !d_quant || !aligned16(d_data) || !aligned16(d_quant)) return FZ_INVALID_ARG;
+    const uint64_t nl = (uint64_t)len3.x * len3.y * len3.z;
+    if (check_dims(nl, len3) != FZ_SUCCESS || !(eb_abs > 0) || !std::isfinite(eb_abs)) return FZ_INVALID_ARG;
+    const double e2 = eb_abs * 2;
+    cudaError_t  e  = launch_lorenzo_construct(d_data, d_quant, d_signum, len3.x, len3.y, len3.z,
+                                               (float)(1 / e2), reinterpret_cast<cudaStream_t>(stream));
+    return map_err(e);
+}
+
+fz_status fz_lorenzo_reconstruct(const uint16_t* d_quant, const uint8_t* d_signum, float* d_xdata,
+                                 fz_dims len3, double eb_abs, fz_stream_t stream)
+{
+    if (!d_quant || !d_xdata || !aligned16(d_quant) || !aligned16(d_xdata)) return FZ_INVALID_ARG;
+    const uint64_t nl = (uint64_t)len3.x * len3.y * len3.z;
+    if (check_dims(nl, len3) != FZ_SUCCESS || !(eb_abs > 0) || !std::isfinite(eb_abs)) return FZ_INVALID_ARG;
+    ReconArgs r{};
+    r.codes = d_quant, r.signbits = nullptr, r.signum = d_signum, r.out = d_xdata;
+    r.n = (uint32_t)nl, r.nl = (uint32_t)nl, r.x = len3.x, r.y = len3.y, r.z = len3.z;
+    r.ebx2 = (float)(eb_abs * 2);
+    return map_err(launch_reconstruct(r, reinterpret_cast<cudaStream_t>(stream)));
+}
+
+fz_status fz_bitshuffle_flag(const uint32_t* d_in, uint32_t* d_out, uint64_t n_codes,
+                             uint32_t* d_bitflag, uint32_t* d_byteflag, fz_stream_t stream)
+{
+    if (!d_in || !d_out || !d_bitflag || !d_byteflag || n_codes == 0 || n_codes > kMaxN) return FZ_INVALID_ARG;
+    if (!aligned16(d_in) || !aligned16(d_out)) return FZ_INVALID_ARG;
+    return map_err(launch_bitshuffle_flag(d_in, d_out, (uint32_t)n_codes, d_bitflag, d_byteflag,
+                                          reinterpret_cast<cudaStream_t>(stream)));
+}
+
+fz_status fz_scan_encode(fz_workspace* ws, const uint8_t* d_shuffled, const uint32_t* d_byteflag,
+                         uint64_t n_codes, uint32_t* d_presum, uint8_t* d_out, uint64_t* nnz,
+                         fz_stream_t stream)
+{
+    if (!ws || !d_shuffled || !d_byteflag || n_codes == 0 || n_codes > ws->max_n) return FZ_INVALID_ARG;
+    if (!aligned16(d_shuffled) || (d_out && !aligned16(d_out))) return FZ_INVALID_ARG;
+    fz_status st = check_device(ws);
+    if (st != FZ_SUCCESS) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t  e = launch_scan_encode(d_shuffled, d_byteflag, (uint32_t)n_codes, d_presum, d_out,
+                                        ws->state, ws->tickets + 2, ws->status, ws->total,
+                                        next_epoch(ws, s), s);
+    if (e != cudaSuccess) return map_err(e);
+    if (nnz) {
+        e = cudaMemcpyAsync(ws->h_pinned, ws->total, 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return map_err(e, FZ_FAIL_GPU_MEMCPY);
+        uint32_t t;
+        std::memcpy(&t, ws->h_pinned, 4);
+        *nnz = t;
+        return fz_workspace_status(ws, stream);
+    }
+    return FZ_SUCCESS;
+}
+
+}  // extern "C"

@@ -1,0 +1,626 @@
+// fz_compress.cu -- compression kernels.
+//
+//   k_range       max - min of the field and the error-bound constants (fz.cu:137,
+//                 lorenzo_var.cuh:562-563), one pass, last-CTA finish.
+//   k_compress    the whole forward path in one pass: Lorenzo dual-quantisation
+//                 (lorenzo_var.cuh:47-295), bitshuffle + chunk flags + bitmap
+//                 (fz.cu:61-111), single-pass decoupled-lookback scan (replacing
+//                 cub::DeviceScan, fz.cu:187-201) and compaction (encodeDebug,
+//                 fz.cu:49-59).  Reads the field once, writes the stream once.
+//
+// Work decomposition: one warp owns one 2048-code shuffle block.  The warp computes its
+// codes from the floats (halo rows come from L2), stages them in 4 KiB of shared memory,
+// transposes 32x32 bit tiles in registers, derives the chunk flags with 8 ballots (which
+// are exactly the 8 bitmap words of the block), finds its output offset by look-back
+// over the preceding blocks and writes its non-zero chunks with 128-bit stores.
+#include "fz_internal.h"
+
+namespace fz {
+
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+// Prequantised values of in[e0+j-off], j=0..3 (0 where e0+j < off or e0+j-off >= lim).
+__device__ __forceinline__ void row4(const float* __restrict__ in, uint32_t e0, uint32_t off,
+                                     uint32_t aligned, uint32_t lim, float r, float (&q)[4])
+{
+    if (aligned && e0 >= off && e0 - off + 3 < lim) {
+        const float4 v = ldg4(in + (e0 - off));
+        q[0] = pq(v.x, r), q[1] = pq(v.y, r), q[2] = pq(v.z, r), q[3] = pq(v.w, r);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t e = e0 + j;
+            q[j] = (e >= off && e - off < lim) ? pq(__ldg(in + (e - off)), r) : 0.0f;
+        }
+    }
+}
+
+__device__ __forceinline__ float west_of(const float* __restrict__ in, uint32_t e0, uint32_t off,
+                                         float r)
+{
+    return e0 >= off + 1 ? pq(__ldg(in + (e0 - 1 - off)), r) : 0.0f;
+}
+
+// Codes of the 4 consecutive elements e0..e0+3 (e0 % 4 == 0).  All 32 lanes of the warp
+// must call this together (the west neighbours come from lane-1 by shuffle).  `lim` is
+// the number of readable input elements; codes at e >= nl are 0.  `ovf` collects
+// "delta does not fit its field"; `sgn` (1D) gets bit j = (delta_j < 0).
+struct Geo {
+    uint32_t nl, x, y, xy, lim;
+    FastDiv  dx, dxy;
+    uint32_t al_x, al_xy, al_xyx;
+};
+
+template <int ND>
+__device__ __forceinline__ void codes4(const float* __restrict__ in, const Geo& g, uint32_t e0,
+                                       float r, uint32_t lane, uint32_t (&code)[4],
+                                       uint32_t& ovf, uint32_t& sgn)
+{
+    float p[4];
+    row4(in, e0, 0, 1, g.lim, r, p);
+    float wp = __shfl_up_sync(kFull, p[3], 1);
+    if (lane == 0) wp = west_of(in, e0, 0, r);
+
+    if constexpr (ND == 1) {
+        // c_lorenzo_1d1l (lorenzo_var.cuh:176-214): 256-element blocks, p[-1] = 0.
+        const uint32_t k = e0 & 255u;
+        float          d[4];
+        d[0] = __fsub_rn(p[0], k ? wp : 0.0f);
+        d[1] = __fsub_rn(p[1], p[0]);
+        d[2] = __fsub_rn(p[2], p[1]);
+        d[3] = __fsub_rn(p[3], p[2]);
+        sgn  = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const bool live = e0 + j < g.nl;
+            code[j]         = live ? (j == 0 ? pack_signed(d[j]) : pack_unsigned(d[j])) : 0u;
+            ovf |= (live && !(fabsf(d[j]) < (j == 0 ? 32768.0f : 65536.0f))) ? 1u : 0u;
+            sgn |= (live && d[j] < 0) ? (1u << j) : 0u;
+        }
+        return;
+    }
+
+    if constexpr (ND == 2) {
+        // c_lorenzo_2d1l_16x16data_mapto16x2 (lorenzo_var.cuh:216-238): 16x16 tiles,
+        // d = (c - n) - (w - nw), zero outside the tile.
+        float nq[4];
+        row4(in, e0, g.x, g.al_x, g.lim, r, nq);
+        float wn = __shfl_up_sync(kFull, nq[3], 1);
+        if (lane == 0) wn = west_of(in, e0, g.x, r);
+        uint32_t row = fdiv(e0, g.dx), col = e0 - row * g.x;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (j) {
+                if (++col == g.x) col = 0, ++row;
+            }
+            const bool  rin = (row & 15u) != 0, cin = (col & 15u) != 0;
+            const float N   = rin ? nq[j] : 0.0f;
+            const float W   = cin ? (j ? p[j - 1] : wp) : 0.0f;
+            const float NW  = (rin && cin) ? (j ? nq[j - 1] : wn) : 0.0f;
+            const float d   = __fsub_rn(__fsub_rn(p[j], N), __fsub_rn(W, NW));
+            const bool  live = e0 + j < g.nl;
+            code[j]          = live ? pack_signed(d) : 0u;
+            ovf |= (live && !(fabsf(d) < 32768.0f)) ? 1u : 0u;
+        }
+        return;
+    }
+
+    if constexpr (ND == 3) {
+        // c_lorenzo_3d1l_32x8x8data_mapto32x1x8 (lorenzo_var.cuh:240-295): 8x8x8 tiles,
+        // the 7-term expression of :277-283 evaluated left to right.
+        float nq[4], bq[4], bn[4];
+        row4(in, e0, g.x, g.al_x, g.lim, r, nq);
+        row4(in, e0, g.xy, g.al_xy, g.lim, r, bq);
+        row4(in, e0, g.xy + g.x, g.al_xyx, g.lim, r, bn);
+        float wn  = __shfl_up_sync(kFull, nq[3], 1);
+        float wb  = __shfl_up_sync(kFull, bq[3], 1);
+        float wbn = __shfl_up_sync(kFull, bn[3], 1);
+        if (lane == 0) {
+            wn  = west_of(in, e0, g.x, r);
+            wb  = west_of(in, e0, g.xy, r);
+            wbn = west_of(in, e0, g.xy + g.x, r);
+        }
+        uint32_t zz = fdiv(e0, g.dxy), rem = e0 - zz * g.xy;
+        uint32_t yy = fdiv(rem, g.dx), xx = rem - yy * g.x;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (j) {
+                if (++xx == g.x) {
+                    xx = 0;
+                    if (++yy == g.y) yy = 0, ++zz;
+                }
+            }
+            const bool  zi = (zz & 7u) != 0, yi = (yy & 7u) != 0, xi = (xx & 7u) != 0;
+            const float A  = (zi && yi && xi) ? (j ? bn[j - 1] : wbn) : 0.0f;
+            const float B  = (yi && xi) ? (j ? nq[j - 1] : wn) : 0.0f;
+            const float Cc = (zi && xi) ? (j ? bq[j - 1] : wb) : 0.0f;
+            const float D  = (zi && yi) ? bn[j] : 0.0f;
+            const float E  = xi ? (j ? p[j - 1] : wp) : 0.0f;
+            const float F  = yi ? nq[j] : 0.0f;
+            const float G  = zi ? bq[j] : 0.0f;
+            float       s  = __fsub_rn(A, B);
+            s              = __fsub_rn(s, Cc);
+            s              = __fsub_rn(s, D);
+            s              = __fadd_rn(s, E);
+            s              = __fadd_rn(s, F);
+            s              = __fadd_rn(s, G);
+            const float d  = __fsub_rn(p[j], s);
+            const bool  live = e0 + j < g.nl;
+            code[j]          = live ? pack_signed(d) : 0u;
+            ovf |= (live && !(fabsf(d) < 32768.0f)) ? 1u : 0u;
+        }
+    }
+}
+
+// --------------------------------------------------------------- range --
+__global__ void __launch_bounds__(256) k_range(const float* __restrict__ in, uint32_t n,
+                                               double eb, int rel, float2* partials,
+                                               uint32_t* ticket, EbInfo* out, uint32_t* status)
+{
+    __shared__ float    smn[8], smx[8];
+    __shared__ uint32_t snf[8];
+    __shared__ bool     last;
+    float          mn = INFINITY, mx = -INFINITY;
+    uint32_t       nonfinite = 0;
+    const uint32_t n4        = n / 4;
+    const uint32_t stride    = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+        const float4 v = ldg4(in + 4 * (size_t)i);
+        mn = fminf(fminf(mn, v.x), fminf(v.y, fminf(v.z, v.w)));
+        mx = fmaxf(fmaxf(mx, v.x), fmaxf(v.y, fmaxf(v.z, v.w)));
+        nonfinite |= !isfinite(v.x) | !isfinite(v.y) | !isfinite(v.z) | !isfinite(v.w);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < n - 4 * n4) {
+        const float v = in[4 * n4 + threadIdx.x];
+        mn = fminf(mn, v), mx = fmaxf(mx, v);
+        nonfinite |= !isfinite(v);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(kFull, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+    }
+    nonfinite = __reduce_or_sync(kFull, nonfinite);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) smn[w] = mn, smx[w] = mx, snf[w] = nonfinite;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < 8; ++i) mn = fminf(mn, smn[i]), mx = fmaxf(mx, smx[i]), nonfinite |= snf[i];
+        partials[blockIdx.x] = make_float2(mn, mx);
+        if (nonfinite) atomicOr(status, kStatusNonfinite);
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    // the last CTA folds the partials and derives the error-bound constants
+    __threadfence();
+    mn = INFINITY, mx = -INFINITY;
+    for (uint32_t i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+        const float2 p = __ldcg(partials + i);
+        mn = fminf(mn, p.x), mx = fmaxf(mx, p.y);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(kFull, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+    }
+    if (lane == 0) smn[w] = mn, smx[w] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < 8; ++i) mn = fminf(mn, smn[i]), mx = fmaxf(mx, smx[i]);
+        EbInfo e;
+        e.vmin  = mn;
+        e.vmax  = mx;
+        e.range = rel ? __fsub_rn(mx, mn) : 0.0f;
+        e.eb_abs = rel ? eb * (double)e.range : eb;  // fz.cu:149 eb * range
+        const double ebx2 = e.eb_abs * 2;             // lorenzo_var.cuh:562
+        e.ebx2_r    = (float)(1 / ebx2);              // lorenzo_var.cuh:563
+        e.ebx2      = (float)ebx2;
+        e.nonfinite = 0;
+        *out        = e;
+        *ticket     = 0;  // ready for the next call
+    }
+}
+
+__global__ void k_set_eb(EbInfo* out, double eb_abs)
+{
+    EbInfo e;
+    e.eb_abs = eb_abs;
+    const double ebx2 = eb_abs * 2;
+    e.ebx2_r = (float)(1 / ebx2);
+    e.ebx2   = (float)ebx2;
+    e.range = e.vmin = e.vmax = 0.0f;
+    e.nonfinite = 0;
+    *out        = e;
+}
+
+// ------------------------------------------------------------ compress --
+constexpr int kCompressWarps = 8;
+
+// Stream header (struct fz_header, include/fz.h), written by the last tile once its
+// inclusive prefix -- the stream's chunk count -- is known.
+__device__ void write_header(const CompressArgs& a, const EbInfo& e, uint32_t ovf, uint32_t nnz)
+{
+    uint8_t* h = a.out;
+    *reinterpret_cast<uint4*>(h + 0)  = make_uint4(0x31475A46u, 1u | (a.mode << 16) | (a.ndim << 24), a.x, a.y);
+    *reinterpret_cast<uint4*>(h + 16) = make_uint4(a.z, ovf ? 1u : 0u, a.n, 0u);
+    const unsigned long long eb = __double_as_longlong(e.eb_abs);
+    *reinterpret_cast<uint4*>(h + 32) = make_uint4((uint32_t)eb, (uint32_t)(eb >> 32), __float_as_uint(e.ebx2_r),
+                                                   __float_as_uint(e.ebx2));
+    *reinterpret_cast<uint4*>(h + 48) = make_uint4(nnz, 0u, __float_as_uint(e.range), a.sidecar_bytes);
+}
+
+// Swizzled position (in u32 words) of 16-byte chunk q of a block's code image: chunk
+// (g, t) of group g lives at g*8 + (t ^ (g & 7)) so that both the row-major writes of
+// the Lorenzo phase and the per-group reads of the transpose are conflict-free.
+__device__ __forceinline__ uint32_t swz(uint32_t q)
+{
+    const uint32_t g = q >> 3, t = q & 7u;
+    return ((g << 3) | (t ^ (g & 7u))) << 2;
+}
+
+template <int ND>
+__global__ void __launch_bounds__(kCompressWarps * 32) k_compress(const CompressArgs a)
+{
+    __shared__ __align__(16) uint32_t smem[kCompressWarps][kBlockWords];
+    __shared__ uint32_t               cta_tile;
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    uint32_t*      sm   = smem[wid];
+
+    // Tiles are handed out in launch order so every predecessor of a tile has started:
+    // the look-back always makes progress.
+    if (threadIdx.x == 0) {
+        const uint32_t c = atomicAdd(a.ticket, 1u);
+        if (c == gridDim.x - 1) atomicExch(a.ticket, 0u);  // last ticket: reset for the next call
+        cta_tile = c;
+    }
+    __syncthreads();
+    const uint32_t t = cta_tile * kCompressWarps + wid;
+    if (t >= a.ntiles) return;
+
+    const EbInfo eb = a.eb ? *a.eb : a.ebh;
+    const float  r  = eb.ebx2_r;
+    Geo         g;
+    g.nl = a.nl, g.x = a.x, g.y = a.y, g.xy = a.xy, g.lim = a.n;
+    g.dx = a.dx, g.dxy = a.dxy, g.al_x = a.al_x, g.al_xy = a.al_xy, g.al_xyx = a.al_xyx;
+
+    const uint32_t base = t * kBlockCodes;
+    uint32_t       ovf  = 0;
+    uint32_t*      signw = (ND == 1 && a.mode == 1)
+                               ? reinterpret_cast<uint32_t*>(a.out + a.off_sign) : nullptr;
+
+    if (t < a.nb) {
+        // ---- phase A: codes of the block into shared memory (swizzled) ----
+#pragma unroll 2
+        for (uint32_t it = 0; it < 16; ++it) {
+            const uint32_t e0 = base + it * 128 + lane * 4;
+            uint32_t       c[4], sgn = 0;
+            codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
+            const uint32_t q = it * 16 + (lane >> 1);
+            *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
+                make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+            if (ND == 1 && signw) {
+                // 4 sign bits per lane -> one u32 per 8 lanes (32 consecutive elements)
+                uint32_t v = sgn << ((lane & 7u) * 4);
+                v |= __shfl_xor_sync(kFull, v, 1);
+                v |= __shfl_xor_sync(kFull, v, 2);
+                v |= __shfl_xor_sync(kFull, v, 4);
+                if ((lane & 7u) == 0) signw[(base >> 5) + it * 4 + (lane >> 3)] = v;
+            }
+        }
+        __syncwarp();
+        // ---- phase B: lane g transposes group g (words g*32 .. g*32+31) ----
+        uint32_t w[32];
+#pragma unroll
+        for (uint32_t tt = 0; tt < 8; ++tt) {
+            const uint4 v = *reinterpret_cast<const uint4*>(sm + swz(lane * 8 + tt));
+            w[4 * tt] = v.x, w[4 * tt + 1] = v.y, w[4 * tt + 2] = v.z, w[4 * tt + 3] = v.w;
+        }
+        transpose32(w);
+        __syncwarp();
+        // shuffled image S[p*32 + g] = w[p] (bitshuffleAndBitflag's out, fz.cu:82)
+#pragma unroll
+        for (uint32_t p = 0; p < 32; ++p) sm[p * 32 + lane] = w[p];
+        __syncwarp();
+        // ---- phase C: chunk c = lane + 32 i; ballot i is bitmap word 8t+i ----
+        uint4    ch[8];
+        uint32_t bm[8], cnt = 0;
+#pragma unroll
+        for (uint32_t i = 0; i < 8; ++i) {
+            ch[i] = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
+            bm[i] = __ballot_sync(kFull, (ch[i].x | ch[i].y | ch[i].z | ch[i].w) != 0);
+            cnt += __popc(bm[i]);
+        }
+        if (lane == 0) {
+            uint4* A = reinterpret_cast<uint4*>(a.out + a.off_a) + 2 * (size_t)t;
+            A[0]     = make_uint4(bm[0], bm[1], bm[2], bm[3]);
+            A[1]     = make_uint4(bm[4], bm[5], bm[6], bm[7]);
+        }
+        ovf = __reduce_or_sync(kFull, ovf);
+        // ---- phase D: offset of this block's chunks (decoupled look-back) ----
+        uint32_t excl = 0, povf = 0;
+        if (t == 0) {
+            if (lane == 0) publish(a.state, 0, a.epoch, kFlagIncl, ovf, cnt);
+        } else {
+            if (lane == 0) publish(a.state, t, a.epoch, kFlagAgg, ovf, cnt);
+            lookback(a.state, t, a.epoch, a.status, excl, povf);
+            if (lane == 0) publish(a.state, t, a.epoch, kFlagIncl, ovf | povf, excl + cnt);
+        }
+        // ---- phase E: compacted 128-bit stores of the non-zero chunks ----
+        uint4*         B   = reinterpret_cast<uint4*>(a.out + a.off_b);
+        const uint32_t lt  = lanemask_lt();
+        uint32_t       pre = excl;
+#pragma unroll
+        for (uint32_t i = 0; i < 8; ++i) {
+            if ((bm[i] >> lane) & 1u) B[pre + __popc(bm[i] & lt)] = ch[i];
+            pre += __popc(bm[i]);
+        }
+        if (t == a.ntiles - 1 && lane == 0) write_header(a, eb, ovf | povf, excl + cnt);
+        return;
+    }
+
+    // ---- tail tile: n mod 2048 codes, never shuffled (fz.cu:173) ----
+    {
+        const uint32_t tail = a.n - base;
+        uint16_t*      tc   = (a.mode == 1) ? reinterpret_cast<uint16_t*>(a.out + a.off_c) : nullptr;
+        for (uint32_t it = 0; it * 128 < tail; ++it) {
+            const uint32_t e0 = base + it * 128 + lane * 4;
+            uint32_t       c[4], sgn = 0;
+            codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (tc && e0 + j < a.n) tc[e0 + j - base] = (uint16_t)c[j];
+            if (ND == 1 && signw) {
+                uint32_t v = sgn << ((lane & 7u) * 4);
+                v |= __shfl_xor_sync(kFull, v, 1);
+                v |= __shfl_xor_sync(kFull, v, 2);
+                v |= __shfl_xor_sync(kFull, v, 4);
+                const uint32_t wi = (base >> 5) + it * 4 + (lane >> 3);
+                if ((lane & 7u) == 0 && wi * 32 < a.n) signw[wi] = v;
+            }
+        }
+        // zero padding of the tail code array and of the sign array
+        if (tc) {
+            for (uint32_t i = tail + lane; i < (uint32_t)(pad16(2 * (uint64_t)tail) / 2); i += 32) tc[i] = 0;
+        }
+        if (ND == 1 && signw) {
+            const uint32_t nsw = (uint32_t)cdiv(a.n, 32);
+            const uint32_t pw  = (uint32_t)(pad16(4 * (uint64_t)nsw) / 4);
+            for (uint32_t i = nsw + lane; i < pw; i += 32) signw[i] = 0;
+        }
+        // bitmap words of the partial block are zero (fz.cu:167), then the 16-byte pad
+        uint32_t*      A  = reinterpret_cast<uint32_t*>(a.out + a.off_a);
+        const uint32_t pa = (uint32_t)(pad16(4 * (uint64_t)a.nwords) / 4);
+        for (uint32_t i = a.nb * 8 + lane; i < pa; i += 32) A[i] = 0;
+        ovf = __reduce_or_sync(kFull, ovf);
+        uint32_t excl = 0, povf = 0;
+        if (t == 0) {
+            if (lane == 0) publish(a.state, 0, a.epoch, kFlagIncl, ovf, 0);
+        } else {
+            if (lane == 0) publish(a.state, t, a.epoch, kFlagAgg, ovf, 0);
+            lookback(a.state, t, a.epoch, a.status, excl, povf);
+            if (lane == 0) publish(a.state, t, a.epoch, kFlagIncl, ovf | povf, excl);
+        }
+        if (lane == 0) write_header(a, eb, ovf | povf, excl);
+    }
+}
+
+// One warp looks back from tile 1 at tile 0, which nothing publishes in this epoch: the
+// bounded wait must give up and raise kStatusTimeout (fz_selftest_wait_timeout).
+__global__ void k_wait_selftest(const uint64_t* state, uint32_t epoch, uint32_t* status)
+{
+    uint32_t excl = 0, ovf = 0;
+    lookback(state, 1, epoch, status, excl, ovf);
+}
+
+cudaError_t launch_wait_selftest(const uint64_t* state, uint32_t epoch, uint32_t* status, cudaStream_t s)
+{
+    k_wait_selftest<<<1, 32, 0, s>>>(state, epoch, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_range(const float* in, uint32_t n, double eb, int rel, float2* partials,
+                         uint32_t* ticket, EbInfo* out, uint32_t* status, cudaStream_t s)
+{
+    k_range<<<kRangeGrid, 256, 0, s>>>(in, n, eb, rel, partials, ticket, out, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_eb(EbInfo* out, double eb_abs, cudaStream_t s)
+{
+    k_set_eb<<<1, 1, 0, s>>>(out, eb_abs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compress(const CompressArgs& a, cudaStream_t s)
+{
+    const uint32_t ctas = (uint32_t)cdiv(a.ntiles, kCompressWarps);
+    switch (a.ndim) {
+    case 1: k_compress<1><<<ctas, kCompressWarps * 32, 0, s>>>(a); break;
+    case 2: k_compress<2><<<ctas, kCompressWarps * 32, 0, s>>>(a); break;
+    default: k_compress<3><<<ctas, kCompressWarps * 32, 0, s>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
+// =================================================== stage-level kernels ==
+// fz_lorenzo_construct: codes of [0, x*y*z) into a u16 array (launch_construct_
+// LorenzoI_var, lorenzo_var.cuh:520-597).  One warp per 128 consecutive elements.
+template <int ND>
+__global__ void __launch_bounds__(256) k_lorenzo_codes(const float* __restrict__ in, uint16_t* q,
+                                                       uint8_t* signum, Geo g, float r)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t e0   = warp * 128 + lane * 4;
+    if (warp * 128 >= g.nl) return;  // warp-uniform
+    uint32_t c[4], ovf = 0, sgn = 0;
+    codes4<ND>(in, g, e0, r, lane, c, ovf, sgn);
+    if (e0 + 3 < g.nl) {
+        *reinterpret_cast<uint2*>(q + e0) = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (e0 + j < g.nl) q[e0 + j] = (uint16_t)c[j];
+    }
+    if (ND == 1 && signum) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (e0 + j < g.nl) signum[e0 + j] = (sgn >> j) & 1u;
+    }
+}
+
+cudaError_t launch_lorenzo_construct(const float* in, uint16_t* q, uint8_t* signum, uint32_t x,
+                                     uint32_t y, uint32_t z, float ebx2_r, cudaStream_t s)
+{
+    Geo g;
+    g.x = x, g.y = y, g.xy = x * y, g.nl = x * y * z, g.lim = g.nl;
+    g.dx = make_fastdiv(x), g.dxy = make_fastdiv(g.xy);
+    g.al_x = (x % 4) == 0, g.al_xy = (g.xy % 4) == 0, g.al_xyx = ((g.xy + x) % 4) == 0;
+    const int      nd    = (z == 1 && y == 1) ? 1 : (z == 1 ? 2 : 3);
+    const uint32_t warps = (uint32_t)cdiv(g.nl, 128);
+    const uint32_t ctas  = (uint32_t)cdiv(warps, 8);
+    if (nd == 1) k_lorenzo_codes<1><<<ctas, 256, 0, s>>>(in, q, signum, g, ebx2_r);
+    else if (nd == 2) k_lorenzo_codes<2><<<ctas, 256, 0, s>>>(in, q, signum, g, ebx2_r);
+    else k_lorenzo_codes<3><<<ctas, 256, 0, s>>>(in, q, signum, g, ebx2_r);
+    return cudaGetLastError();
+}
+
+// fz_bitshuffle_flag: bitshuffleAndBitflag over floor(n/2048) blocks (fz.cu:61-111)
+// plus the raw tail copy (fz.cu:155) and zeroed flags past the last full block.
+__global__ void __launch_bounds__(256) k_bitshuffle(const uint32_t* __restrict__ in, uint32_t* out,
+                                                    uint32_t n_codes, uint32_t* bitflag,
+                                                    uint32_t* byteflag)
+{
+    __shared__ __align__(16) uint32_t smem[8][kBlockWords];
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const uint32_t t    = blockIdx.x * 8 + wid;
+    const uint32_t nb   = n_codes / kBlockCodes;
+    const uint32_t nw   = (uint32_t)cdiv(n_codes, 256);
+    uint32_t*      sm   = smem[wid];
+    if (t < nb) {
+        const uint4* src = reinterpret_cast<const uint4*>(in + (size_t)t * kBlockWords);
+#pragma unroll
+        for (uint32_t i = 0; i < 8; ++i) {
+            const uint32_t q = lane + 32 * i;
+            *reinterpret_cast<uint4*>(sm + swz(q)) = src[q];
+        }
+        __syncwarp();
+        uint32_t w[32];
+#pragma unroll
+        for (uint32_t tt = 0; tt < 8; ++tt) {
+            const uint4 v = *reinterpret_cast<const uint4*>(sm + swz(lane * 8 + tt));
+            w[4 * tt] = v.x, w[4 * tt + 1] = v.y, w[4 * tt + 2] = v.z, w[4 * tt + 3] = v.w;
+        }
+        transpose32(w);
+        __syncwarp();
+#pragma unroll
+        for (uint32_t p = 0; p < 32; ++p) sm[p * 32 + lane] = w[p];
+        __syncwarp();
+        uint4* dst = reinterpret_cast<uint4*>(out + (size_t)t * kBlockWords);
+#pragma unroll
+        for (uint32_t i = 0; i < 8; ++i) {
+            const uint4 v = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
+            dst[lane + 32 * i] = v;
+            const bool f = (v.x | v.y | v.z | v.w) != 0;
+            byteflag[(size_t)t * kChunks + lane + 32 * i] = f;
+            const uint32_t b = __ballot_sync(kFull, f);
+            if (lane == 0) bitflag[(size_t)t * 8 + i] = b;
+        }
+        return;
+    }
+    if (t == nb) {
+        // tail: raw copy of the remaining bytes (2n total) and zero flags
+        const uint8_t* s8 = reinterpret_cast<const uint8_t*>(in);
+        uint8_t*       d8 = reinterpret_cast<uint8_t*>(out);
+        for (uint64_t b = (uint64_t)nb * 4096 + lane; b < 2ull * n_codes; b += 32) d8[b] = s8[b];
+        for (uint32_t i = nb * 8 + lane; i < nw; i += 32) bitflag[i] = 0;
+        for (uint32_t i = nb * kChunks + lane; i < 32 * nw; i += 32) byteflag[i] = 0;
+    }
+}
+
+cudaError_t launch_bitshuffle_flag(const uint32_t* in, uint32_t* out, uint32_t n_codes,
+                                   uint32_t* bitflag, uint32_t* byteflag, cudaStream_t s)
+{
+    const uint32_t tiles = n_codes / kBlockCodes + 1;
+    k_bitshuffle<<<(uint32_t)cdiv(tiles, 8), 256, 0, s>>>(in, out, n_codes, bitflag, byteflag);
+    return cudaGetLastError();
+}
+
+// fz_scan_encode: exclusive scan of M u32 flags (cub::DeviceScan::ExclusiveSum,
+// fz.cu:187-192) + total (fz.cu:194-201) + compaction (encodeDebug, fz.cu:49-59).
+// One warp per 256 flags, decoupled look-back across warps.
+__global__ void __launch_bounds__(256) k_scan_encode(const uint8_t* __restrict__ shuffled,
+                                                     const uint32_t* __restrict__ flags,
+                                                     uint32_t n_codes, uint32_t m,
+                                                     uint32_t* presum, uint8_t* out,
+                                                     uint64_t* state, uint32_t* ticket,
+                                                     uint32_t* status, uint32_t* total,
+                                                     uint32_t epoch)
+{
+    __shared__ uint32_t cta_tile;
+    const uint32_t      lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        const uint32_t c = atomicAdd(ticket, 1u);
+        if (c == gridDim.x - 1) atomicExch(ticket, 0u);
+        cta_tile = c;
+    }
+    __syncthreads();
+    const uint32_t t      = cta_tile * 8 + wid;
+    const uint32_t ntiles = m / 256;  // m = 32 * ceil(n/256), a multiple of 32; tiles of 256
+    const uint32_t ntl    = (m + 255) / 256;
+    if (t >= ntl) return;
+    (void)ntiles;
+    uint32_t bm[8], cnt = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < 8; ++i) {
+        const uint32_t idx = t * 256 + 32 * i + lane;
+        bm[i] = __ballot_sync(kFull, idx < m && flags[idx] != 0);
+        cnt += __popc(bm[i]);
+    }
+    uint32_t excl = 0, povf = 0;
+    if (t == 0) {
+        if (lane == 0) publish(state, 0, epoch, kFlagIncl, 0, cnt);
+    } else {
+        if (lane == 0) publish(state, t, epoch, kFlagAgg, 0, cnt);
+        lookback(state, t, epoch, status, excl, povf);
+        if (lane == 0) publish(state, t, epoch, kFlagIncl, 0, excl + cnt);
+    }
+    const uint32_t lt       = lanemask_lt();
+    uint32_t       pre      = excl;
+    const uint64_t srcbytes = 2ull * n_codes;
+#pragma unroll
+    for (uint32_t i = 0; i < 8; ++i) {
+        const uint32_t idx  = t * 256 + 32 * i + lane;
+        const uint32_t rank = pre + __popc(bm[i] & lt);
+        if (presum && idx < m) presum[idx] = rank;
+        if ((bm[i] >> lane) & 1u && out) {
+            const uint64_t b0 = 16ull * idx;
+            if (b0 + 16 <= srcbytes) {
+                reinterpret_cast<uint4*>(out)[rank] = reinterpret_cast<const uint4*>(shuffled)[idx];
+            } else {
+                for (int k = 0; k < 16; ++k) out[16ull * rank + k] = b0 + k < srcbytes ? shuffled[b0 + k] : 0;
+            }
+        }
+        pre += __popc(bm[i]);
+    }
+    if (t == ntl - 1 && lane == 0) {
+        if (presum) presum[m] = pre;
+        *total = pre;
+    }
+}
+
+cudaError_t launch_scan_encode(const uint8_t* shuffled, const uint32_t* byteflag,
+                               uint32_t n_codes, uint32_t* presum, uint8_t* out,
+                               uint64_t* state, uint32_t* ticket, uint32_t* status,
+                               uint32_t* total, uint32_t epoch, cudaStream_t s)
+{
+    const uint32_t m     = 32u * (uint32_t)cdiv(n_codes, 256);
+    const uint32_t tiles = (uint32_t)cdiv(m, 256);
+    k_scan_encode<<<(uint32_t)cdiv(tiles, 8), 256, 0, s>>>(shuffled, byteflag, n_codes, m, presum,
+                                                           out, state, ticket, status, total, epoch);
+    return cudaGetLastError();
+}
+
+}  // namespace fz

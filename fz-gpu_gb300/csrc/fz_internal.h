@@ -1,0 +1,85 @@
+// fz_internal.h -- host-side declarations shared by the .cu files of the library.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fz_device.cuh"
+
+namespace fz {
+
+__host__ __device__ inline uint64_t cdiv(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
+__host__ __device__ inline uint64_t pad16(uint64_t a) { return (a + 15) & ~uint64_t(15); }
+
+// Geometry of one field and its stream.
+struct Layout {
+    uint32_t n, nl, x, y, z, xy, ndim;
+    uint32_t nb;       // full shuffle blocks
+    uint32_t tail;     // n - 2048 nb
+    uint32_t nwords;   // bitmap words ceil(n/256)
+    uint32_t mode;
+    uint64_t off_a, off_c, off_b, off_sign;  // byte offsets in the stream
+    uint32_t sidecar_bytes;
+};
+Layout make_layout(uint64_t n, uint32_t x, uint32_t y, uint32_t z, uint32_t mode);
+
+// Arguments of the fused compression kernel.
+struct CompressArgs {
+    const float* in;
+    uint8_t*     out;
+    uint32_t     n, nl, x, y, z, xy;
+    FastDiv      dx, dxy;
+    uint32_t     al_x, al_xy, al_xyx;  // 1 when the halo row offsets are multiples of 4
+    uint32_t     nb, ntiles, nwords, mode, ndim, sidecar_bytes;
+    uint64_t     off_a, off_c, off_b, off_sign;
+    const EbInfo* eb;   // device constants from the range pass (relative eb), or null
+    EbInfo       ebh;   // constants computed on the host (absolute eb)
+    uint64_t*    state;
+    uint32_t*    ticket;
+    uint32_t*    status;
+    uint32_t     epoch;
+};
+
+struct DecodeArgs {
+    const uint8_t* st;
+    uint16_t*      codes;  // scratch u16[n]
+    uint32_t       n, nb, tail, mode;
+    uint64_t       off_a, off_c, off_b, nnz;
+    uint64_t*      state;
+    uint32_t*      ticket;
+    uint32_t*      status;
+    uint32_t       epoch;
+};
+
+struct ReconArgs {
+    const uint16_t* codes;
+    const uint32_t* signbits;  // 1D sign bits (nullable)
+    const uint8_t*  signum;    // 1D per-element signs (nullable; stage API)
+    float*          out;
+    uint32_t        n, nl, x, y, z;
+    float           ebx2;
+};
+
+// launchers (return the launch error)
+cudaError_t launch_range(const float* in, uint32_t n, double eb, int rel, float2* partials,
+                         uint32_t* ticket, EbInfo* out, uint32_t* status, cudaStream_t s);
+cudaError_t launch_set_eb(EbInfo* out, double eb_abs, cudaStream_t s);
+cudaError_t launch_compress(const CompressArgs& a, cudaStream_t s);
+cudaError_t launch_decode(const DecodeArgs& a, cudaStream_t s);
+cudaError_t launch_reconstruct(const ReconArgs& a, cudaStream_t s);
+
+cudaError_t launch_wait_selftest(const uint64_t* state, uint32_t epoch, uint32_t* status, cudaStream_t s);
+
+// stage-level launchers
+cudaError_t launch_lorenzo_construct(const float* in, uint16_t* q, uint8_t* signum, uint32_t x,
+                                     uint32_t y, uint32_t z, float ebx2_r, cudaStream_t s);
+cudaError_t launch_bitshuffle_flag(const uint32_t* in, uint32_t* out, uint32_t n_codes,
+                                   uint32_t* bitflag, uint32_t* byteflag, cudaStream_t s);
+cudaError_t launch_scan_encode(const uint8_t* shuffled, const uint32_t* byteflag,
+                               uint32_t n_codes, uint32_t* presum, uint8_t* out,
+                               uint64_t* state, uint32_t* ticket, uint32_t* status,
+                               uint32_t* total, uint32_t epoch, cudaStream_t s);
+
+constexpr int kRangeGrid = 608;  // 4 CTAs per SM on 152 SMs
+
+}  // namespace fz

@@ -1,0 +1,226 @@
+/*
+ * fz.h -- C ABI of the GB300-native FZ compression pipeline.
+ *
+ * The reference (FZ-GPU) exposes its hot path at three boundaries; each entry point
+ * below names the reference interface it replaces:
+ *   - the CLI / host orchestration  runSzs() ................. fz.cu:113-224
+ *   - the C++ launchers  launch_{construct,reconstruct}_LorenzoI_var
+ *                                                  include/kernel/lorenzo_var.cuh:520-673
+ *   - the raw kernels  bitshuffleAndBitflag / cub::DeviceScan::ExclusiveSum / encodeDebug
+ *                                                  fz.cu:49-111, fz.cu:187-205
+ * The status enum keeps the values of the reference's C-ABI error enum
+ * (include/cusz/type.h:25-44) and adds codes for stream and launch failures.
+ *
+ * Conventions
+ *   - Every device-buffer entry point is stream-ordered: it enqueues work on `stream`
+ *     and returns without synchronising, unless an optional host output (marked
+ *     "host, nullable, syncs") is requested.
+ *   - Buffers are caller-owned. Device pointers must be 16-byte aligned.
+ *   - Nothing here calls exit(); every failure is a returned fz_status.
+ *   - A workspace holds the scan state of one in-flight call. Use one workspace per
+ *     stream (or per host thread); concurrent calls on one workspace race.
+ *   - Sizes are 64-bit. Dimensions are (x, y, z) with x fastest, as the reference's
+ *     dim3 len3 (fz.cu:116, 231-233).  One field holds at most 2^31 elements (the
+ *     reference's int sizes cap it at 2^29, fz.cu:117-118).
+ */
+#ifndef FZ_GB300_FZ_H
+#define FZ_GB300_FZ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cudaStream_t without pulling in CUDA headers (same underlying type). */
+typedef struct CUstream_st* fz_stream_t;
+
+/* ---------------------------------------------------------------- status -- */
+typedef enum fz_status {
+    FZ_SUCCESS                  = 0x00, /* CUSZ_SUCCESS */
+    FZ_FAIL_ONDISK_FILE_ERROR   = 0x01, /* CUSZ_FAIL_ONDISK_FILE_ERROR */
+    FZ_FAIL_DATA_NOT_READY      = 0x02, /* CUSZ_FAIL_DATA_NOT_READY */
+    FZ_FAIL_GPU_MALLOC          = 0x03, /* CUSZ_FAIL_GPU_MALLOC */
+    FZ_FAIL_GPU_MEMCPY          = 0x04, /* CUSZ_FAIL_GPU_MEMCPY */
+    FZ_FAIL_GPU_ILLEGAL_ACCESS  = 0x05, /* CUSZ_FAIL_GPU_ILLEGAL_ACCESS: any launch/runtime error */
+    FZ_FAIL_GPU_OUT_OF_MEMORY   = 0x06, /* CUSZ_FAIL_GPU_OUT_OF_MEMORY */
+    FZ_FAIL_INCOMPRESSIABLE     = 0x07, /* CUSZ_FAIL_INCOMPRESSIABLE */
+    FZ_FAIL_UNSUPPORTED_DATATYPE = 0x08,
+    FZ_NOT_IMPLEMENTED          = 0x0100, /* CUSZ_NOT_IMPLEMENTED */
+    /* codes without a reference counterpart */
+    FZ_INVALID_ARG              = 0x0200, /* bad pointer/size/dims/eb */
+    FZ_CORRUPT_STREAM           = 0x0201, /* header or section sizes inconsistent */
+    FZ_OUT_OF_SPACE             = 0x0202, /* output capacity too small */
+    FZ_TIMEOUT                  = 0x0203, /* a bounded device-side wait gave up */
+    FZ_NO_DEVICE                = 0x0204, /* no CUDA device / driver */
+    FZ_NONFINITE_INPUT          = 0x0205  /* NaN/Inf in a relative-eb input */
+} fz_status;
+
+/* ------------------------------------------------------------- constants -- */
+#define FZ_MAGIC            0x31475A46u /* "FZG1" little-endian */
+#define FZ_FORMAT_VERSION   1u
+#define FZ_HEADER_BYTES     64u
+#define FZ_BLOCK_CODES      2048u /* codes per shuffle block: grid floor(N/2048), fz.cu:173 */
+#define FZ_BLOCK_WORDS      1024u /* u32 words per shuffle block, fz.cu:73 */
+#define FZ_CHUNK_BYTES      16u   /* blockSize, fz.cu:157 */
+#define FZ_CHUNKS_PER_BLOCK 256u  /* 4 KiB / 16 B */
+#define FZ_CODES_PER_WORD   256u  /* codes covered by one bitmap word (32 chunks x 8 codes) */
+
+/* header flags */
+/* some delta did not fit its code field (|d| >= 32768 signed, >= 65536 for 1D unsigned
+   positions, or non-finite): the stream does not meet the error bound there */
+#define FZ_FLAG_CODE_OVERFLOW 0x1u
+
+typedef enum fz_mode {
+    /* Sections A+B only: the reference's exact compressed content. Not invertible
+       for the tail codes (N mod 2048) or for 1D signs at i%4!=0. */
+    FZ_MODE_COMPAT = 0,
+    /* Sections A+B unchanged, plus a fixed-size Section C holding the raw tail codes
+       and (1D only) every delta's sign bit, so decompression meets the error bound. */
+    FZ_MODE_SIDECAR = 1
+} fz_mode;
+
+typedef enum fz_eb_mode {
+    FZ_EB_ABS = 0, /* eb is absolute (launch_construct_LorenzoI_var's eb, lorenzo_var.cuh:526) */
+    FZ_EB_REL = 1  /* eb is relative to max-min of the input (fz.cu:137,149) */
+} fz_eb_mode;
+
+typedef struct fz_dims {
+    uint32_t x, y, z; /* x fastest; ndim = 1 if y==z==1, 2 if z==1, else 3 */
+} fz_dims;
+
+/* 64-byte little-endian stream header.  Stream layout:
+ *   [header 64 B][Section A: u32 bitmap[ceil(n/256)], padded to 16 B]
+ *   [Section C: sidecar_bytes][Section B: nnz x 16 B chunks]
+ * Sections A and B hold exactly the reference's d_bitFlagArray[0..ceil(n/256)) and
+ * d_out[0..16*nnz) (fz.cu:109, fz.cu:57). */
+typedef struct fz_header {
+    uint32_t magic;
+    uint16_t version;
+    uint8_t  mode;     /* fz_mode */
+    uint8_t  ndim;
+    uint32_t x, y, z;
+    uint32_t flags;    /* FZ_FLAG_* */
+    uint64_t n;        /* element count = file bytes / 4 (fz.cu:118) */
+    double   eb_abs;   /* absolute error bound */
+    float    ebx2_r;   /* (float)(1 / (2 eb_abs)), lorenzo_var.cuh:562-563 */
+    float    ebx2;     /* (float)(2 eb_abs), lorenzo_var.cuh:641 */
+    uint64_t nnz;      /* non-zero 16-byte chunks in Section B */
+    float    range;    /* max - min of the input (0 in FZ_EB_ABS mode) */
+    uint32_t sidecar_bytes;
+} fz_header;
+
+typedef struct fz_workspace fz_workspace;
+
+/* ------------------------------------------------------------ utilities -- */
+const char* fz_status_string(fz_status s);
+const char* fz_version(void);
+/* Number of dimensions the reference's launcher dispatches on (lorenzo_var.cuh:537-544). */
+int fz_ndim(fz_dims dims);
+
+/* Byte offsets of the sections of a stream for `n` elements. */
+fz_status fz_stream_layout(uint64_t n, fz_dims dims, fz_mode mode, uint64_t* off_a,
+                           uint64_t* off_c, uint64_t* off_b, uint32_t* sidecar_bytes);
+/* Worst-case stream size (every chunk non-zero). */
+fz_status fz_max_compressed_bytes(uint64_t n, fz_dims dims, fz_mode mode, uint64_t* bytes);
+/* Total stream bytes implied by a header (validates it). */
+fz_status fz_stream_bytes(const fz_header* h, uint64_t* bytes);
+/* The three numbers runSzs prints (fz.cu:207-209): file size, 4*ceil(n/256) + 16*nnz,
+   and their ratio. */
+fz_status fz_reference_sizes(uint64_t file_bytes, uint64_t nnz, uint64_t* original,
+                             uint64_t* compressed, double* ratio);
+
+/* ------------------------------------------------------------ workspace -- */
+/* Device scratch for fields of up to max_n elements (scan state, range reduction,
+   decode scratch) plus a pinned host word for optional readbacks. */
+fz_status fz_workspace_create(uint64_t max_n, fz_workspace** ws);
+fz_status fz_workspace_destroy(fz_workspace* ws);
+/* Device bytes a workspace for max_n elements allocates. */
+fz_status fz_workspace_bytes(uint64_t max_n, uint64_t* bytes);
+/* Device-side status of the last call on this workspace (syncs `stream`):
+   FZ_SUCCESS, FZ_TIMEOUT or FZ_NONFINITE_INPUT. Clears it. */
+fz_status fz_workspace_status(fz_workspace* ws, fz_stream_t stream);
+
+/* Per-kernel timing, the counterpart of the reference launcher's time_elapsed
+   out-parameter (lorenzo_var.cuh:527,568-596).  Once enabled, each kernel launch made
+   by a call on this workspace (up to `capacity` launches in total) is bracketed by a
+   pair of CUDA events on the call's stream.  capacity 0 disables it. */
+fz_status fz_workspace_enable_timing(fz_workspace* ws, uint32_t capacity);
+/* Number of recorded launches of one kernel kind (0 range pass, 1 fused compress,
+   2 decode, 3 inverse Lorenzo) and their summed duration; syncs on the last recorded
+   event and frees those records. */
+fz_status fz_workspace_kernel_time(fz_workspace* ws, int kind, uint32_t* launches,
+                                   double* total_ms);
+
+/* Diagnostic: launches one warp whose look-back waits on a tile that nothing
+   publishes.  The bounded wait gives up after its poll limit (about a second) and the
+   call returns FZ_TIMEOUT; any other result means the wait bound is broken.  No
+   reference counterpart (the reference's only device-wide step is a CUB scan). */
+fz_status fz_selftest_wait_timeout(fz_workspace* ws, fz_stream_t stream);
+
+/* ------------------------------------------------ full pipeline, device -- */
+/* Compress d_in[0..n) (dims describe the first x*y*z elements; n may exceed it as
+   in fz.cu:117-118) into d_out.  Replaces runSzs (fz.cu:113-224) minus file I/O.
+   out_bytes: host, nullable, syncs -- the stream's total size. */
+fz_status fz_compress(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims dims,
+                      double eb, fz_eb_mode eb_mode, fz_mode mode, void* d_out,
+                      uint64_t out_capacity, uint64_t* out_bytes, fz_stream_t stream);
+
+/* Decompress a stream produced by fz_compress into d_out[0..n).  h_header is the
+   stream's header copied to host memory (the caller usually has it already; pass
+   NULL to have it read back, which syncs).  No reference counterpart: the
+   reference has no working FZ decompressor; this is the inverse of fz_compress. */
+fz_status fz_decompress(fz_workspace* ws, const void* d_stream, uint64_t stream_bytes,
+                        const fz_header* h_header, float* d_out, uint64_t out_capacity_elems,
+                        fz_stream_t stream);
+
+/* ------------------------------------------------- full pipeline, host -- */
+/* Same as above with host buffers: H2D of the input, compress, D2H of the stream;
+   synchronous.  The device staging buffers live in the workspace (allocated on the
+   first call, sized for its max_n).  h_in/h_out should be pinned for full bandwidth.
+   This is what the fz-gpu CLI calls (fz.cu:136-209). */
+fz_status fz_compress_host(fz_workspace* ws, const float* h_in, uint64_t n, fz_dims dims,
+                           double eb, fz_eb_mode eb_mode, fz_mode mode, void* h_out,
+                           uint64_t out_capacity, uint64_t* out_bytes, fz_stream_t stream);
+fz_status fz_decompress_host(fz_workspace* ws, const void* h_stream, uint64_t stream_bytes,
+                             float* h_out, uint64_t out_capacity_elems, fz_stream_t stream);
+
+/* ------------------------------------------------ stage-level drop-ins -- */
+/* Lorenzo dual-quantisation into 16-bit sign-magnitude codes; replaces
+   launch_construct_LorenzoI_var<float,uint16_t,float> (lorenzo_var.cuh:520-597).
+   Writes d_quant[i] for i < x*y*z only (fz.cu:145 pre-zeroes the rest).  The 1D
+   sign of every delta is written to d_signum[i] (0/1) when d_signum is non-NULL; the
+   reference leaves signum unused (fz.cu:152). */
+fz_status fz_lorenzo_construct(const float* d_data, uint16_t* d_quant, uint8_t* d_signum,
+                               fz_dims len3, double eb_abs, fz_stream_t stream);
+
+/* Inverse of the above for sign-magnitude codes; replaces
+   launch_reconstruct_LorenzoI_var (lorenzo_var.cuh:599-673), whose input format
+   (separate signum + magnitude) the compressor never produces.  1D: d_signum (0/1
+   per element, nullable) supplies the signs that the codes at i%4!=0 lack. */
+fz_status fz_lorenzo_reconstruct(const uint16_t* d_quant, const uint8_t* d_signum,
+                                 float* d_xdata, fz_dims len3, double eb_abs,
+                                 fz_stream_t stream);
+
+/* Bitshuffle of n_codes 16-bit codes (viewed as u32 words) in 4 KiB blocks with
+   16-byte chunk flags and a 1-bit-per-chunk bitmap; replaces bitshuffleAndBitflag
+   (fz.cu:61-111) and its grid floor(N/2048) (fz.cu:172-174).  Words past the last
+   full block are copied unchanged (fz.cu:155).  d_byteflag: u32[32*ceil(n/256)],
+   d_bitflag: u32[ceil(n/256)], both fully written (zero past the last full block). */
+fz_status fz_bitshuffle_flag(const uint32_t* d_in, uint32_t* d_out, uint64_t n_codes,
+                             uint32_t* d_bitflag, uint32_t* d_byteflag, fz_stream_t stream);
+
+/* Exclusive prefix sum of the chunk flags plus compaction of the flagged 16-byte
+   chunks; replaces cub::DeviceScan::ExclusiveSum + the total fix-up + encodeDebug
+   (fz.cu:187-205).  d_presum (nullable) receives P[0..M] with M = 32*ceil(n/256)
+   (fz.cu:180); d_out must hold 16*M bytes, as the reference's d_out does (fz.cu:165);
+   nnz: host, nullable, syncs. */
+fz_status fz_scan_encode(fz_workspace* ws, const uint8_t* d_shuffled,
+                         const uint32_t* d_byteflag, uint64_t n_codes, uint32_t* d_presum,
+                         uint8_t* d_out, uint64_t* nnz, fz_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FZ_GB300_FZ_H */

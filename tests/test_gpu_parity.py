@@ -1,0 +1,231 @@
+"""GPU parity: the sm_103a kernels, called through the C ABI, against the oracle.
+
+Streams must be byte-identical, codes/flags/offsets bit-exact and reconstructions
+bit-identical to the oracle's; reconstructions must also meet the error bound
+|x - x'| <= eb (1 + 2^-21) + 2^-21 |x| at every point."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import error_tolerance
+
+pytestmark = pytest.mark.gpu
+
+BIG = 1 << 25  # workspace capacity: covers the 25M-element 3D workload
+
+
+@pytest.fixture(scope="module")
+def ws(fz):
+    torch.cuda.set_device(0)
+    return fz.Workspace(BIG)
+
+
+def run_both(fz, oracle, ws, data, dims, eb, rel=True, mode=1):
+    xt = torch.from_numpy(np.ascontiguousarray(data)).cuda()
+    st = fz.compress(xt, dims, eb, rel=rel, mode=mode, ws=ws)
+    got = st.cpu().numpy()
+    want = oracle.compress(data, dims, eb, rel=rel, mode=mode)
+    return st, got, want
+
+
+def assert_same_stream(got, want):
+    assert got.size == want.size, f"stream size {got.size} != oracle {want.size}"
+    bad = np.nonzero(got != want)[0]
+    assert bad.size == 0, f"{bad.size} bytes differ, first at {bad[:8]}"
+
+
+SMALL = [
+    ("smooth2d", (300, 70, 1), 1e-3), ("peaks2d", (400, 90, 1), 1e-4), ("smooth2d", (101, 37, 1), 1e-3),
+    ("smooth2d", (1, 3000, 1), 1e-3), ("smooth2d", (17, 2049, 1), 1e-2), ("smooth3d", (40, 33, 20), 1e-3),
+    ("smooth3d", (37, 19, 11), 1e-2), ("smooth3d", (33, 1, 70), 1e-3), ("smooth3d", (9, 9, 9), 1e-3),
+    ("smooth1d", (100000, 1, 1), 1e-3), ("smooth1d", (1500, 1, 1), 1e-3), ("smooth1d", (2048, 1, 1), 1e-3),
+    ("smooth1d", (4097, 1, 1), 1e-4), ("smooth2d", (64, 32, 1), 1e-3), ("smooth1d", (7, 1, 1), 1e-3),
+]
+
+
+@pytest.mark.parametrize("kind,dims,eb", SMALL, ids=[f"{k}-{'x'.join(map(str, d))}-{e}" for k, d, e in SMALL])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_compress_decompress_small(fz, oracle, synth, ws, kind, dims, eb, mode):
+    data = synth.field(kind, dims, seed=hash((kind, dims)) % 1000)
+    st, got, want = run_both(fz, oracle, ws, data, dims, eb, mode=mode)
+    assert_same_stream(got, want)
+    rec = fz.decompress(st, ws=ws).cpu().numpy()
+    rec_o = oracle.decompress(want)
+    assert np.array_equal(rec.view(np.uint32), rec_o.view(np.uint32))
+    if mode == 1:
+        h = oracle.parse_header(want)
+        assert (np.abs(rec.astype(np.float64) - data) <= error_tolerance(data, h["eb_abs"])).all()
+
+
+FULL = [
+    ("cesm-like 3600x1800", "smooth2d", (3600, 1800, 1), 0, 1e-3),
+    ("exafel-like 39200x388", "peaks2d", (39200, 388, 1), 1, 1e-3),
+    ("exafel-like 39200x388", "peaks2d", (39200, 388, 1), 1, 1e-4),
+    ("hurricane-like 500x500x100", "smooth3d", (500, 500, 100), 2, 1e-2),
+    ("hurricane-like 500x500x100", "smooth3d", (500, 500, 100), 2, 1e-3),
+    ("hurricane-like 500x500x100", "smooth3d", (500, 500, 100), 2, 1e-4),
+]
+
+
+@pytest.mark.parametrize("name,kind,dims,seed,eb", FULL, ids=[f"{f[0].split()[0]}-{f[4]}" for f in FULL])
+def test_full_size_workloads(fz, oracle, synth, ws, name, kind, dims, seed, eb):
+    data = synth.field(kind, dims, seed)
+    st, got, want = run_both(fz, oracle, ws, data, dims, eb, mode=1)
+    assert_same_stream(got, want)
+    rec = fz.decompress(st, ws=ws).cpu().numpy()
+    rec_o = oracle.decompress(want)
+    assert np.array_equal(rec.view(np.uint32), rec_o.view(np.uint32))
+    h = oracle.parse_header(want)
+    assert (np.abs(rec.astype(np.float64) - data) <= error_tolerance(data, h["eb_abs"])).all()
+    m = oracle.metrics(data, rec)
+    assert m["max_abs_err"] <= h["eb_abs"] * (1 + 2 ** -10)
+    print(f"{name} eb={eb}: nnz={h['nnz']} ratio(ref)={fz.reference_sizes(4 * data.size, h['nnz'])[2]:.3f} "
+          f"psnr={m['psnr']:.2f} max_err/eb={m['max_abs_err'] / h['eb_abs']:.6f}")
+
+
+def test_absolute_eb_and_len_longer_than_dims(fz, oracle, synth, ws):
+    d = np.concatenate([synth.smooth2d(64, 64, seed=18), np.linspace(-1, 1, 777, dtype=np.float32)])
+    for rel, eb in [(False, 0.004), (True, 1e-3)]:
+        st, got, want = run_both(fz, oracle, ws, d, (64, 64, 1), eb, rel=rel)
+        assert_same_stream(got, want)
+        rec = fz.decompress(st, ws=ws).cpu().numpy()
+        assert np.array_equal(rec.view(np.uint32), oracle.decompress(want).view(np.uint32))
+        assert not rec[64 * 64:].any()
+
+
+def crafted(vals, nd):
+    if nd == 2:
+        g = np.zeros((16, 16 * vals.size), np.float32)
+        g[0, ::16] = vals
+        g[5, 3::16] = vals[::-1]
+        return g.ravel(), (16 * vals.size, 16, 1)
+    if nd == 1:
+        g = np.zeros(256 * vals.size, np.float32)
+        g[::256] = vals
+        g[131::256] = vals[::-1]
+        return g, (g.size, 1, 1)
+    g = np.zeros((8, 8, 8 * vals.size), np.float32)
+    g[0, 0, ::8] = vals
+    g[3, 2, 5::8] = vals[::-1]
+    return g.ravel(), (8 * vals.size, 8, 8)
+
+
+LIMITS = np.array([0, 1, -1, 2.5, -2.5, 0.5, -0.5, 1.5, 30000, 32767, 32768, -32768, 40000, 65535,
+                   65536, -65536, 70000, -70000, 1e6, -1e9, 3e38, np.inf, -np.inf, np.nan, -np.nan,
+                   12345.5, -0.0, 7, 100000, 32767.5, 65535.5, 65534.7], np.float32)
+
+
+@pytest.mark.parametrize("nd", [1, 2, 3])
+def test_code_field_limits_and_nonfinite(fz, oracle, ws, nd):
+    """Deltas at and beyond the 15/16-bit code fields, Inf and NaN (absolute eb 0.5,
+    ebx2_r = 1): codes and the overflow flag match the oracle bit for bit."""
+    data, dims = crafted(LIMITS, nd)
+    st, got, want = run_both(fz, oracle, ws, data, dims, 0.5, rel=False)
+    assert_same_stream(got, want)
+    assert oracle.parse_header(want)["flags"] & 1
+    rec = fz.decompress(st, ws=ws).cpu().numpy()
+    assert np.array_equal(rec.view(np.uint32), oracle.decompress(want).view(np.uint32))
+
+
+def test_stage_lorenzo_construct_reconstruct(fz, oracle, synth, ws):
+    for kind, dims, eb in [("smooth2d", (300, 70, 1), 1e-3), ("smooth3d", (37, 19, 11), 1e-2),
+                           ("smooth1d", (5000, 1, 1), 1e-3), ("peaks2d", (513, 33, 1), 1e-4)]:
+        data = synth.field(kind, dims, seed=3)
+        eb_abs = eb * float(np.float32(data.max() - data.min()))
+        xt = torch.from_numpy(data).cuda()
+        q, sg = fz.lorenzo_construct(xt, dims, eb_abs, signum=True)
+        codes, sgo, _ = oracle.lorenzo_construct(data, dims, oracle.ebx2_r(eb_abs), signum=True)
+        assert np.array_equal(q.cpu().numpy().view(np.uint16), codes)
+        if dims[1] == 1 and dims[2] == 1:
+            assert np.array_equal(sg.cpu().numpy(), sgo)
+        rec = fz.lorenzo_reconstruct(q, dims, eb_abs, signum=sg).cpu().numpy()
+        sb = np.packbits(sgo, bitorder="little") if dims[1] == 1 and dims[2] == 1 else None
+        rec_o = oracle.lorenzo_reconstruct(codes, dims, oracle.ebx2(eb_abs), sb)
+        assert np.array_equal(rec.view(np.uint32), rec_o.view(np.uint32))
+
+
+@pytest.mark.parametrize("n", [100, 2048, 5000, 3 * 2048 + 17, 40000])
+def test_stage_bitshuffle_scan_encode(fz, oracle, ws, n):
+    rng = np.random.default_rng(n)
+    codes = (rng.random(n) < 0.05).astype(np.uint16) * rng.integers(1, 60000, n).astype(np.uint16)
+    ct = torch.from_numpy(codes.view(np.int16)).cuda()
+    sh, bit, byte = fz.bitshuffle_flag(ct)
+    S, F, B = oracle.bitshuffle_flag(codes)
+    assert np.array_equal(sh.cpu().numpy().view(np.uint16), S.view(np.uint16)[:n])
+    assert np.array_equal(byte.cpu().numpy().view(np.uint32), F)
+    assert np.array_equal(bit.cpu().numpy().view(np.uint32), B)
+    pad = torch.zeros(2 * ((n + 1) // 2) + 16, dtype=torch.int16, device="cuda")
+    pad[:n] = sh
+    pre, out, nnz = fz.scan_encode(pad, byte, n, ws=ws)
+    P, outo, nnzo = oracle.scan_encode(S, F, n)
+    assert nnz == nnzo
+    assert np.array_equal(pre.cpu().numpy().view(np.uint32), P)
+    assert np.array_equal(out.cpu().numpy(), outo)
+
+
+def test_host_buffer_path_matches_device_path(fz, oracle, synth, ws):
+    data = synth.smooth3d(60, 50, 40, seed=4)
+    st_h = fz.compress_host(data, (60, 50, 40), 1e-3, ws=ws)
+    want = oracle.compress(data, (60, 50, 40), 1e-3)
+    assert_same_stream(st_h, want)
+    rec = fz.decompress_host(st_h, ws=ws)
+    assert np.array_equal(rec.view(np.uint32), oracle.decompress(want).view(np.uint32))
+
+
+def test_workspace_reuse_across_calls(fz, oracle, synth, ws):
+    """Epoch-tagged scan state: back-to-back calls of different sizes on one workspace."""
+    fields = [(synth.smooth2d(500, 300, seed=i), (500, 300, 1)) for i in range(2)]
+    fields += [(synth.smooth1d(30000, seed=9), (30000, 1, 1)), (synth.smooth3d(30, 30, 30, seed=2), (30, 30, 30))]
+    for rep in range(3):
+        for data, dims in fields:
+            st, got, want = run_both(fz, oracle, ws, data, dims, 1e-3)
+            assert_same_stream(got, want)
+
+
+def test_errors_are_statuses(fz, ws):
+    x = torch.zeros(4096 + 4, device="cuda")
+    out = torch.empty(1 << 16, dtype=torch.uint8, device="cuda")
+    with pytest.raises(fz.FzError) as e:
+        fz.compress(x[1:4097], (4096, 1, 1), 1e-3, ws=ws, out=out)  # misaligned input
+    assert e.value.status == fz.INVALID_ARG
+    with pytest.raises(fz.FzError) as e:
+        fz.compress(x[:4096], (4096, 1, 1), 1e-3, ws=ws, out=out[:100])
+    assert e.value.status == fz.OUT_OF_SPACE
+    with pytest.raises(fz.FzError) as e:
+        fz.compress(x[:4096], (64, 65, 1), 1e-3, ws=ws)  # x*y*z > n
+    assert e.value.status == fz.INVALID_ARG
+    with pytest.raises(fz.FzError) as e:
+        fz.compress(x[:4096], (4096, 1, 1), -1.0, ws=ws)
+    assert e.value.status == fz.INVALID_ARG
+    y = torch.ones(5000, device="cuda")
+    y[77] = float("nan")
+    with pytest.raises(fz.FzError) as e:
+        fz.compress(y, (5000, 1, 1), 1e-3, rel=True, ws=ws)
+    assert e.value.status == fz.NONFINITE_INPUT
+    # the workspace stays usable after an error status
+    st = fz.compress(torch.linspace(0, 1, 5000, device="cuda"), (5000, 1, 1), 1e-3, ws=ws)
+    assert st.numel() > 64
+
+
+def test_corrupt_stream_is_detected(fz, oracle, synth, ws):
+    data = synth.smooth2d(300, 70, seed=1)
+    want = oracle.compress(data, (300, 70, 1), 1e-3)
+    st = torch.from_numpy(want.copy()).cuda()
+    bad = st.clone()
+    bad[64:64 + 32] = 255  # bitmap of block 0 claims 256 chunks
+    h = fz.parse_header(want)
+    fz.decompress(bad, header=h, ws=ws)       # stream-ordered: the kernel flags it
+    assert ws.status() == fz.CORRUPT_STREAM   # sticky until read
+    assert ws.status() == fz.SUCCESS
+    short = st[: want.size - 16]
+    with pytest.raises(fz.FzError) as e:
+        fz.decompress(short, header=h, ws=ws)
+    assert e.value.status == fz.CORRUPT_STREAM
+
+
+def test_bounded_wait_times_out_without_fault(fz, ws):
+    """A look-back on a tile that never publishes gives up and reports FZ_TIMEOUT; the
+    context stays usable."""
+    assert ws.selftest_wait_timeout() == fz.TIMEOUT
+    st = fz.compress(torch.linspace(0, 1, 9000, device="cuda"), (9000, 1, 1), 1e-3, ws=ws)
+    assert st.numel() > 64
