@@ -69,15 +69,16 @@ float fzo_ebx2_r(double eb_abs)
 /* lorenzo_var.cuh:641: the inverse scales by ebx2, passed as FP=float. */
 float fzo_ebx2(double eb_abs) { return (float)(eb_abs * 2); }
 
-/* static_cast<uint16_t>(fabs(delta)) on the device (lorenzo_var.cuh:53,169,289): a
-   float-to-integer conversion rounding toward zero and clamped to the destination
-   range, NaN to 0.  Pinned against the reference kernels' own output on the GPU
-   (tests/golden, crafted overflow fixture). */
+/* static_cast<uint16_t>(fabs(delta)) as the device evaluates it (lorenzo_var.cuh:53,169,
+   289): a float-to-u32 conversion rounding toward zero that clamps to [0, 2^32-1] and
+   maps NaN to 0, then the low 16 bits.  So |d| = 70000 gives 4464 and Inf gives 0xFFFF.
+   Pinned by the reference kernels' own output on a GB300 (the crafted-limits
+   fixtures in tests/golden). */
 uint16_t fzo_f2u16(float v)
 {
-    if (!(v > 0.0f)) return 0; /* +-0 and NaN */
-    if (v >= 65535.0f) return 65535;
-    return (uint16_t)v;
+    if (!(v > 0.0f)) return 0;                  /* +-0 and NaN */
+    if (v >= 4294967296.0f) return 0xFFFFu;     /* clamps to 2^32 - 1 */
+    return (uint16_t)((uint32_t)v & 0xFFFFu);
 }
 
 /* Prequantisation, lorenzo_var.cuh:81,125,265: round(data * ebx2_r) in float, ties away

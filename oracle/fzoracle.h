@@ -26,7 +26,8 @@ void fzo_value_range(const float* data, uint64_t n, float* mn, float* mx);
 float fzo_ebx2_r(double eb_abs);
 float fzo_ebx2(double eb_abs);
 
-/* Device conversion (uint16_t)fabsf(d) (lorenzo_var.cuh:53,169,289) for d >= 0 or NaN. */
+/* Device conversion (uint16_t)fabsf(d) (lorenzo_var.cuh:53,169,289) for d >= 0 or NaN:
+   saturating float->u32, then the low 16 bits. */
 uint16_t fzo_f2u16(float v);
 
 /* Dual-quant Lorenzo codes, lorenzo_var.cuh:47-295.  codes[0..n) fully written;

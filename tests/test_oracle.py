@@ -64,7 +64,7 @@ def py_codes(data, dims, r):
 
     def pack(d, signed=True):
         a = abs(float(d))
-        m = 0 if not a > 0 else (65535 if a >= 65535 else int(a))
+        m = 0 if not a > 0 else (0xFFFF if a >= 2.0 ** 32 else int(a) & 0xFFFF)
         return (m | ((d < 0) << 15)) & 0xFFFF if signed else m
 
     out = np.zeros(data.size, np.uint16)
@@ -102,6 +102,7 @@ def test_lorenzo_matches_per_element_restatement(oracle, dims):
     rng = np.random.default_rng(sum(dims))
     n = dims[0] * dims[1] * dims[2] + 5
     data = (rng.normal(0, 1, n) * 50).astype(np.float32)
+    data[rng.random(n) < 0.02] = np.float32(1e6)   # deltas past the 16-bit field
     data[rng.random(n) < 0.2] = 0
     r = oracle.ebx2_r(0.01)
     codes, _, _ = oracle.lorenzo_construct(data, dims, r)
@@ -133,9 +134,13 @@ def test_lorenzo_known_answers(oracle):
     for v, ovf in [(32767.0, 0), (32768.0, 1), (-32767.0, 0)]:
         c, _, o = oracle.lorenzo_construct(np.array([v, 0], np.float32), (1, 2, 1), r)
         assert o == ovf
-    assert oracle.lib().fzo_f2u16(np.float32(70000)) == 65535
-    assert oracle.lib().fzo_f2u16(np.float32(np.nan)) == 0
-    assert oracle.lib().fzo_f2u16(np.float32(65534.9)) == 65534
+    # the device conversion (pinned by tests/golden/*crafted*): saturating f32 -> u32,
+    # then the low 16 bits
+    f2u16 = oracle.lib().fzo_f2u16
+    assert f2u16(np.float32(70000)) == 4464 and f2u16(np.float32(1e9)) == 51712
+    assert f2u16(np.float32(65536)) == 0 and f2u16(np.float32(65535.9)) == 65535
+    assert f2u16(np.float32(np.inf)) == 0xFFFF and f2u16(np.float32(1e10)) == 0xFFFF
+    assert f2u16(np.float32(np.nan)) == 0 and f2u16(np.float32(65534.9)) == 65534
 
 
 @pytest.mark.parametrize("kind,dims,eb", [
