@@ -52,8 +52,8 @@ struct fz_workspace {
     uint32_t* tickets;  // [0] compress, [1] decode, [2] scan-encode, [3] range
     uint32_t* status;
     uint32_t* total;
-    float2*   partials;
-    EbInfo*   eb;
+    uint32_t* mm;       // two range accumulator pairs (min, max as ordered u32)
+    uint32_t  range_calls;
     uint16_t* codes;
     uint32_t  epoch;
     uint8_t*  h_pinned;  // 64-byte header + status word
@@ -244,8 +244,7 @@ fz_status fz_workspace_bytes(uint64_t max_n, uint64_t* bytes)
     uint64_t       b     = 0;
     b += pad16(8 * tiles);          // state
     b += 64;                        // tickets, status, total
-    b += pad16(8 * kRangeGrid);     // partials
-    b += pad16(sizeof(EbInfo));     // eb
+    b += 16;                        // range accumulators
     b += pad16(2 * max_n + 16);     // decode scratch
     *bytes = b;
     return FZ_SUCCESS;
@@ -276,10 +275,13 @@ fz_status fz_workspace_create(uint64_t max_n, fz_workspace** out)
     ws->status  = ws->tickets + 4;
     ws->total   = ws->tickets + 5;
     p += 64;
-    ws->partials = reinterpret_cast<float2*>(p), p += pad16(8 * kRangeGrid);
-    ws->eb       = reinterpret_cast<EbInfo*>(p), p += pad16(sizeof(EbInfo));
+    ws->mm       = reinterpret_cast<uint32_t*>(p), p += 16;
     ws->codes    = reinterpret_cast<uint16_t*>(p);
     e            = cudaMemset(ws->d_base, 0, bytes);
+    if (e == cudaSuccess) {
+        const uint32_t init[4] = {0xFFFFFFFFu, 0u, 0xFFFFFFFFu, 0u};  // empty min/max
+        e                      = cudaMemcpy(ws->mm, init, sizeof(init), cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMallocHost((void**)&ws->h_pinned, 128);
     if (e != cudaSuccess) {
         cudaFree(ws->d_base);
@@ -389,11 +391,13 @@ fz_status fz_compress(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims d
     a.epoch = next_epoch(ws, s);
     cudaError_t e = cudaSuccess;
     if (eb_mode == FZ_EB_REL) {
-        KernelTimer t(ws, s, 0);
-        e    = launch_range(d_in, L.n, eb, 1, ws->partials, ws->tickets + 3, ws->eb, ws->status, s);
-        a.eb = ws->eb;
+        KernelTimer     t(ws, s, 0);
+        const uint32_t  slot = (ws->range_calls++) & 1u;
+        e                    = launch_range(d_in, L.n, ws->mm + 2 * slot, ws->mm + 2 * (slot ^ 1u), ws->status, s);
+        a.mm                 = ws->mm + 2 * slot;
+        a.eb_rel             = eb;
     } else {
-        a.eb            = nullptr;
+        a.mm            = nullptr;
         a.ebh.eb_abs    = eb;
         const double e2 = eb * 2;  // lorenzo_var.cuh:562-563
         a.ebh.ebx2_r    = (float)(1 / e2);

@@ -13,6 +13,8 @@
 // transposes 32x32 bit tiles in registers, derives the chunk flags with 8 ballots (which
 // are exactly the 8 bitmap words of the block), finds its output offset by look-back
 // over the preceding blocks and writes its non-zero chunks with 128-bit stores.
+#include <algorithm>
+
 #include "fz_internal.h"
 
 namespace fz {
@@ -51,11 +53,95 @@ struct Geo {
     uint32_t al_x, al_xy, al_xyx;
 };
 
+// Fast variants for the common case, chosen warp-uniformly: all four elements live and
+// rows a multiple of 4 elements long (so no row starts inside a group and halo rows are
+// 16-byte aligned).  Same float expressions as the generic code below.
+__device__ __forceinline__ void fast2d(const float* __restrict__ in, const Geo& g, uint32_t e0, float r,
+                                       uint32_t lane, uint32_t (&code)[4], uint32_t& ovf)
+{
+    const float4   v   = ldg4(in + e0);
+    const uint32_t row = fdiv(e0, g.dx), col = e0 - row * g.x;
+    const bool     rin = (row & 15u) != 0, cin = (col & 15u) != 0;
+    float4         u   = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (rin) u = ldg4(in + (e0 - g.x));
+    // t = c - n per element: pred2d's first step (lorenzo_var.cuh:140); the west
+    // neighbour's t is what pred2d shuffles in (lorenzo_var.cuh:141)
+    float t[4];
+    t[0] = __fsub_rn(pq(v.x, r), rin ? pq(u.x, r) : 0.0f);
+    t[1] = __fsub_rn(pq(v.y, r), rin ? pq(u.y, r) : 0.0f);
+    t[2] = __fsub_rn(pq(v.z, r), rin ? pq(u.z, r) : 0.0f);
+    t[3] = __fsub_rn(pq(v.w, r), rin ? pq(u.w, r) : 0.0f);
+    float tw = __shfl_up_sync(kFull, t[3], 1);
+    if (lane == 0 && cin)
+        tw = __fsub_rn(pq(__ldg(in + e0 - 1), r), rin ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f);
+    tw = cin ? tw : 0.0f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float d = __fsub_rn(t[j], j ? t[j - 1] : tw);
+        code[j]       = pack_signed(d);
+        ovf |= !(fabsf(d) < 32768.0f) ? 1u : 0u;
+    }
+}
+
+__device__ __forceinline__ void fast3d(const float* __restrict__ in, const Geo& g, uint32_t e0, float r,
+                                       uint32_t lane, uint32_t (&code)[4], uint32_t& ovf)
+{
+    const float4   v  = ldg4(in + e0);
+    const uint32_t zz = fdiv(e0, g.dxy), rem = e0 - zz * g.xy;
+    const uint32_t yy = fdiv(rem, g.dx), xx = rem - yy * g.x;
+    const bool     zi = (zz & 7u) != 0, yi = (yy & 7u) != 0, xi = (xx & 7u) != 0;
+    const float4   z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    // halo rows, zero where the tile has no such neighbour
+    const float4 un = yi ? ldg4(in + (e0 - g.x)) : z4;
+    const float4 ub = zi ? ldg4(in + (e0 - g.xy)) : z4;
+    const float4 uc = (zi && yi) ? ldg4(in + (e0 - g.xy - g.x)) : z4;
+    float        p[4]  = {pq(v.x, r), pq(v.y, r), pq(v.z, r), pq(v.w, r)};
+    float        nq[4] = {pq(un.x, r), pq(un.y, r), pq(un.z, r), pq(un.w, r)};
+    float        bq[4] = {pq(ub.x, r), pq(ub.y, r), pq(ub.z, r), pq(ub.w, r)};
+    float        bn[4] = {pq(uc.x, r), pq(uc.y, r), pq(uc.z, r), pq(uc.w, r)};
+    float        wp = __shfl_up_sync(kFull, p[3], 1), wn = __shfl_up_sync(kFull, nq[3], 1);
+    float        wb = __shfl_up_sync(kFull, bq[3], 1), wbn = __shfl_up_sync(kFull, bn[3], 1);
+    if (lane == 0 && xi) {
+        wp  = pq(__ldg(in + e0 - 1), r);
+        wn  = yi ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f;
+        wb  = zi ? pq(__ldg(in + e0 - 1 - g.xy), r) : 0.0f;
+        wbn = (zi && yi) ? pq(__ldg(in + e0 - 1 - g.xy - g.x), r) : 0.0f;
+    }
+    if (!xi) wp = wn = wb = wbn = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        // c - (A - B - C - D + E + F + G), lorenzo_var.cuh:277-283
+        float s = __fsub_rn(j ? bn[j - 1] : wbn, j ? nq[j - 1] : wn);
+        s       = __fsub_rn(s, j ? bq[j - 1] : wb);
+        s       = __fsub_rn(s, bn[j]);
+        s       = __fadd_rn(s, j ? p[j - 1] : wp);
+        s       = __fadd_rn(s, nq[j]);
+        s       = __fadd_rn(s, bq[j]);
+        const float d = __fsub_rn(p[j], s);
+        code[j]       = pack_signed(d);
+        ovf |= !(fabsf(d) < 32768.0f) ? 1u : 0u;
+    }
+}
+
 template <int ND>
 __device__ __forceinline__ void codes4(const float* __restrict__ in, const Geo& g, uint32_t e0,
                                        float r, uint32_t lane, uint32_t (&code)[4],
                                        uint32_t& ovf, uint32_t& sgn)
 {
+    // warp-uniform choice of the fast variant (the shuffles need all 32 lanes)
+    const bool fast = __all_sync(kFull, e0 + 3 < g.nl) && (ND == 1 || g.al_x);
+    if constexpr (ND == 2) {
+        if (fast) {
+            fast2d(in, g, e0, r, lane, code, ovf);
+            return;
+        }
+    }
+    if constexpr (ND == 3) {
+        if (fast) {
+            fast3d(in, g, e0, r, lane, code, ovf);
+            return;
+        }
+    }
     float p[4];
     row4(in, e0, 0, 1, g.lim, r, p);
     float wp = __shfl_up_sync(kFull, p[3], 1);
@@ -153,22 +239,31 @@ __device__ __forceinline__ void codes4(const float* __restrict__ in, const Geo& 
 }
 
 // --------------------------------------------------------------- range --
-__global__ void __launch_bounds__(256) k_range(const float* __restrict__ in, uint32_t n,
-                                               double eb, int rel, float2* partials,
-                                               uint32_t* ticket, EbInfo* out, uint32_t* status)
+// max and min of the field (fz.cu:137) as order-preserving integers folded with one
+// atomicMin/atomicMax per CTA into mm[0..1].  The other accumulator pair (used by the
+// previous call) is reset here for the next one.  Four 16-byte loads in flight per
+// thread; NaN/Inf raise kStatusNonfinite.
+__global__ void __launch_bounds__(256) k_range(const float* __restrict__ in, uint32_t n, uint32_t* mm,
+                                               uint32_t* mm_next, uint32_t* status)
 {
-    __shared__ float    smn[8], smx[8];
-    __shared__ uint32_t snf[8];
-    __shared__ bool     last;
+    __shared__ uint32_t smn[8], smx[8], snf[8];
+    if (blockIdx.x == 0 && threadIdx.x == 0) mm_next[0] = 0xFFFFFFFFu, mm_next[1] = 0u;
     float          mn = INFINITY, mx = -INFINITY;
     uint32_t       nonfinite = 0;
     const uint32_t n4        = n / 4;
-    const uint32_t stride    = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
-        const float4 v = ldg4(in + 4 * (size_t)i);
-        mn = fminf(fminf(mn, v.x), fminf(v.y, fminf(v.z, v.w)));
-        mx = fmaxf(fmaxf(mx, v.x), fmaxf(v.y, fmaxf(v.z, v.w)));
-        nonfinite |= !isfinite(v.x) | !isfinite(v.y) | !isfinite(v.z) | !isfinite(v.w);
+    const uint32_t per       = blockDim.x * 4;
+    for (uint32_t b = blockIdx.x * per + threadIdx.x; b < n4; b += gridDim.x * per) {
+        float4 v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (b + k * blockDim.x < n4) v[k] = ldg4(in + 4 * (size_t)(b + k * blockDim.x));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (b + k * blockDim.x >= n4) continue;
+            mn = fminf(fminf(mn, v[k].x), fminf(v[k].y, fminf(v[k].z, v[k].w)));
+            mx = fmaxf(fmaxf(mx, v[k].x), fmaxf(v[k].y, fmaxf(v[k].z, v[k].w)));
+            nonfinite |= !isfinite(v[k].x) | !isfinite(v[k].y) | !isfinite(v[k].z) | !isfinite(v[k].w);
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x < n - 4 * n4) {
         const float v = in[4 * n4 + threadIdx.x];
@@ -182,57 +277,36 @@ __global__ void __launch_bounds__(256) k_range(const float* __restrict__ in, uin
     }
     nonfinite = __reduce_or_sync(kFull, nonfinite);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) smn[w] = mn, smx[w] = mx, snf[w] = nonfinite;
+    if (lane == 0) smn[w] = f2ord(mn), smx[w] = f2ord(mx), snf[w] = nonfinite;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int i = 1; i < 8; ++i) mn = fminf(mn, smn[i]), mx = fmaxf(mx, smx[i]), nonfinite |= snf[i];
-        partials[blockIdx.x] = make_float2(mn, mx);
-        if (nonfinite) atomicOr(status, kStatusNonfinite);
-        __threadfence();
-        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (!last) return;
-    // the last CTA folds the partials and derives the error-bound constants
-    __threadfence();
-    mn = INFINITY, mx = -INFINITY;
-    for (uint32_t i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
-        const float2 p = __ldcg(partials + i);
-        mn = fminf(mn, p.x), mx = fmaxf(mx, p.y);
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        mn = fminf(mn, __shfl_xor_sync(kFull, mn, o));
-        mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
-    }
-    if (lane == 0) smn[w] = mn, smx[w] = mx;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int i = 1; i < 8; ++i) mn = fminf(mn, smn[i]), mx = fmaxf(mx, smx[i]);
-        EbInfo e;
-        e.vmin  = mn;
-        e.vmax  = mx;
-        e.range = rel ? __fsub_rn(mx, mn) : 0.0f;
-        e.eb_abs = rel ? eb * (double)e.range : eb;  // fz.cu:149 eb * range
-        const double ebx2 = e.eb_abs * 2;             // lorenzo_var.cuh:562
-        e.ebx2_r    = (float)(1 / ebx2);              // lorenzo_var.cuh:563
-        e.ebx2      = (float)ebx2;
-        e.nonfinite = 0;
-        *out        = e;
-        *ticket     = 0;  // ready for the next call
+    if (threadIdx.x < 32) {
+        const uint32_t nw = blockDim.x >> 5;
+        const uint32_t a  = __reduce_min_sync(kFull, lane < nw ? smn[lane] : 0xFFFFFFFFu);
+        const uint32_t c  = __reduce_max_sync(kFull, lane < nw ? smx[lane] : 0u);
+        const uint32_t f  = __reduce_or_sync(kFull, lane < nw ? snf[lane] : 0u);
+        if (lane == 0) {
+            atomicMin(mm, a);
+            atomicMax(mm + 1, c);
+            if (f) atomicOr(status, kStatusNonfinite);
+        }
     }
 }
 
-__global__ void k_set_eb(EbInfo* out, double eb_abs)
+// Error-bound constants from the range, as runSzs and the launcher derive them:
+// eb = rel * range in double (fz.cu:149), ebx2_r = (float)(1/(2 eb))
+// (lorenzo_var.cuh:562-563), ebx2 = (float)(2 eb) (lorenzo_var.cuh:641).
+__device__ EbInfo eb_from_range(float vmin, float vmax, double rel)
 {
     EbInfo e;
-    e.eb_abs = eb_abs;
-    const double ebx2 = eb_abs * 2;
-    e.ebx2_r = (float)(1 / ebx2);
-    e.ebx2   = (float)ebx2;
-    e.range = e.vmin = e.vmax = 0.0f;
-    e.nonfinite = 0;
-    *out        = e;
+    e.vmin            = vmin;
+    e.vmax            = vmax;
+    e.range           = __fsub_rn(vmax, vmin);
+    e.eb_abs          = rel * (double)e.range;
+    const double ebx2 = e.eb_abs * 2;
+    e.ebx2_r          = (float)(1 / ebx2);
+    e.ebx2            = (float)ebx2;
+    e.nonfinite       = 0;
+    return e;
 }
 
 // ------------------------------------------------------------ compress --
@@ -264,31 +338,34 @@ template <int ND>
 __global__ void __launch_bounds__(kCompressWarps * 32) k_compress(const CompressArgs a)
 {
     __shared__ __align__(16) uint32_t smem[kCompressWarps][kBlockWords];
-    __shared__ uint32_t               cta_tile;
+    __shared__ uint32_t               s_cnt[kCompressWarps], s_ovf[kCompressWarps];
+    __shared__ uint32_t               cta_tile, s_excl;
+    __shared__ EbInfo                 s_eb;
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     uint32_t*      sm   = smem[wid];
 
-    // Tiles are handed out in launch order so every predecessor of a tile has started:
-    // the look-back always makes progress.
+    // Scan tiles are CTAs (8 shuffle blocks), handed out in launch order so that every
+    // predecessor of a tile has started: the look-back always makes progress.
     if (threadIdx.x == 0) {
         const uint32_t c = atomicAdd(a.ticket, 1u);
         if (c == gridDim.x - 1) atomicExch(a.ticket, 0u);  // last ticket: reset for the next call
         cta_tile = c;
+        s_eb     = a.mm ? eb_from_range(ord2f(__ldcg(a.mm)), ord2f(__ldcg(a.mm + 1)), a.eb_rel) : a.ebh;
     }
     __syncthreads();
-    const uint32_t t = cta_tile * kCompressWarps + wid;
-    if (t >= a.ntiles) return;
+    const uint32_t ct = cta_tile;
+    const uint32_t t  = ct * kCompressWarps + wid;  // this warp's shuffle block
 
-    const EbInfo eb = a.eb ? *a.eb : a.ebh;
+    const EbInfo eb = s_eb;
     const float  r  = eb.ebx2_r;
-    Geo         g;
+    Geo          g;
     g.nl = a.nl, g.x = a.x, g.y = a.y, g.xy = a.xy, g.lim = a.n;
     g.dx = a.dx, g.dxy = a.dxy, g.al_x = a.al_x, g.al_xy = a.al_xy, g.al_xyx = a.al_xyx;
 
-    const uint32_t base = t * kBlockCodes;
-    uint32_t       ovf  = 0;
-    uint32_t*      signw = (ND == 1 && a.mode == 1)
-                               ? reinterpret_cast<uint32_t*>(a.out + a.off_sign) : nullptr;
+    const uint32_t base  = t * kBlockCodes;
+    uint32_t       ovf   = 0, cnt = 0;
+    uint32_t       bm[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t*      signw = (ND == 1 && a.mode == 1) ? reinterpret_cast<uint32_t*>(a.out + a.off_sign) : nullptr;
 
     if (t < a.nb) {
         // ---- phase A: codes of the block into shared memory (swizzled) ----
@@ -324,12 +401,10 @@ __global__ void __launch_bounds__(kCompressWarps * 32) k_compress(const Compress
         for (uint32_t p = 0; p < 32; ++p) sm[p * 32 + lane] = w[p];
         __syncwarp();
         // ---- phase C: chunk c = lane + 32 i; ballot i is bitmap word 8t+i ----
-        uint4    ch[8];
-        uint32_t bm[8], cnt = 0;
 #pragma unroll
         for (uint32_t i = 0; i < 8; ++i) {
-            ch[i] = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
-            bm[i] = __ballot_sync(kFull, (ch[i].x | ch[i].y | ch[i].z | ch[i].w) != 0);
+            const uint4 v = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
+            bm[i] = __ballot_sync(kFull, (v.x | v.y | v.z | v.w) != 0);
             cnt += __popc(bm[i]);
         }
         if (lane == 0) {
@@ -337,31 +412,8 @@ __global__ void __launch_bounds__(kCompressWarps * 32) k_compress(const Compress
             A[0]     = make_uint4(bm[0], bm[1], bm[2], bm[3]);
             A[1]     = make_uint4(bm[4], bm[5], bm[6], bm[7]);
         }
-        ovf = __reduce_or_sync(kFull, ovf);
-        // ---- phase D: offset of this block's chunks (decoupled look-back) ----
-        uint32_t excl = 0, povf = 0;
-        if (t == 0) {
-            if (lane == 0) publish(a.state, 0, a.epoch, kFlagIncl, ovf, cnt);
-        } else {
-            if (lane == 0) publish(a.state, t, a.epoch, kFlagAgg, ovf, cnt);
-            lookback(a.state, t, a.epoch, a.status, excl, povf);
-            if (lane == 0) publish(a.state, t, a.epoch, kFlagIncl, ovf | povf, excl + cnt);
-        }
-        // ---- phase E: compacted 128-bit stores of the non-zero chunks ----
-        uint4*         B   = reinterpret_cast<uint4*>(a.out + a.off_b);
-        const uint32_t lt  = lanemask_lt();
-        uint32_t       pre = excl;
-#pragma unroll
-        for (uint32_t i = 0; i < 8; ++i) {
-            if ((bm[i] >> lane) & 1u) B[pre + __popc(bm[i] & lt)] = ch[i];
-            pre += __popc(bm[i]);
-        }
-        if (t == a.ntiles - 1 && lane == 0) write_header(a, eb, ovf | povf, excl + cnt);
-        return;
-    }
-
-    // ---- tail tile: n mod 2048 codes, never shuffled (fz.cu:173) ----
-    {
+    } else if (t == a.nb && a.n > base) {
+        // ---- tail block: n mod 2048 codes, never shuffled (fz.cu:173) ----
         const uint32_t tail = a.n - base;
         uint16_t*      tc   = (a.mode == 1) ? reinterpret_cast<uint16_t*>(a.out + a.off_c) : nullptr;
         for (uint32_t it = 0; it * 128 < tail; ++it) {
@@ -381,9 +433,8 @@ __global__ void __launch_bounds__(kCompressWarps * 32) k_compress(const Compress
             }
         }
         // zero padding of the tail code array and of the sign array
-        if (tc) {
+        if (tc)
             for (uint32_t i = tail + lane; i < (uint32_t)(pad16(2 * (uint64_t)tail) / 2); i += 32) tc[i] = 0;
-        }
         if (ND == 1 && signw) {
             const uint32_t nsw = (uint32_t)cdiv(a.n, 32);
             const uint32_t pw  = (uint32_t)(pad16(4 * (uint64_t)nsw) / 4);
@@ -393,16 +444,42 @@ __global__ void __launch_bounds__(kCompressWarps * 32) k_compress(const Compress
         uint32_t*      A  = reinterpret_cast<uint32_t*>(a.out + a.off_a);
         const uint32_t pa = (uint32_t)(pad16(4 * (uint64_t)a.nwords) / 4);
         for (uint32_t i = a.nb * 8 + lane; i < pa; i += 32) A[i] = 0;
-        ovf = __reduce_or_sync(kFull, ovf);
-        uint32_t excl = 0, povf = 0;
-        if (t == 0) {
-            if (lane == 0) publish(a.state, 0, a.epoch, kFlagIncl, ovf, 0);
+    }
+
+    // ---- phase D: CTA total, then the CTA's offset by decoupled look-back ----
+    ovf = __reduce_or_sync(kFull, ovf);
+    if (lane == 0) s_cnt[wid] = cnt, s_ovf[wid] = ovf;
+    __syncthreads();
+    if (wid == 0) {
+        const uint32_t c   = lane < kCompressWarps ? s_cnt[lane] : 0u;
+        const uint32_t o   = lane < kCompressWarps ? s_ovf[lane] : 0u;
+        const uint32_t tot = __reduce_add_sync(kFull, c);
+        const uint32_t tov = __reduce_or_sync(kFull, o);
+        uint32_t       excl = 0, povf = 0;
+        if (ct == 0) {
+            if (lane == 0) publish(a.state, 0, a.epoch, kFlagIncl, tov, tot);
         } else {
-            if (lane == 0) publish(a.state, t, a.epoch, kFlagAgg, ovf, 0);
-            lookback(a.state, t, a.epoch, a.status, excl, povf);
-            if (lane == 0) publish(a.state, t, a.epoch, kFlagIncl, ovf | povf, excl);
+            if (lane == 0) publish(a.state, ct, a.epoch, kFlagAgg, tov, tot);
+            lookback(a.state, ct, a.epoch, a.status, excl, povf);
+            if (lane == 0) publish(a.state, ct, a.epoch, kFlagIncl, tov | povf, excl + tot);
         }
-        if (lane == 0) write_header(a, eb, ovf | povf, excl);
+        if (lane == 0) {
+            s_excl = excl;
+            if (ct == gridDim.x - 1) write_header(a, eb, tov | povf, excl + tot);
+        }
+    }
+    __syncthreads();
+    if (t >= a.nb || cnt == 0) return;
+
+    // ---- phase E: compacted 128-bit stores of the non-zero chunks ----
+    uint32_t pre = s_excl;
+    for (uint32_t w2 = 0; w2 < wid; ++w2) pre += s_cnt[w2];
+    uint4*         B  = reinterpret_cast<uint4*>(a.out + a.off_b);
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (uint32_t i = 0; i < 8; ++i) {
+        if ((bm[i] >> lane) & 1u) B[pre + __popc(bm[i] & lt)] = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
+        pre += __popc(bm[i]);
     }
 }
 
@@ -420,21 +497,17 @@ cudaError_t launch_wait_selftest(const uint64_t* state, uint32_t epoch, uint32_t
     return cudaGetLastError();
 }
 
-cudaError_t launch_range(const float* in, uint32_t n, double eb, int rel, float2* partials,
-                         uint32_t* ticket, EbInfo* out, uint32_t* status, cudaStream_t s)
+cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* mm_next,
+                         uint32_t* status, cudaStream_t s)
 {
-    k_range<<<kRangeGrid, 256, 0, s>>>(in, n, eb, rel, partials, ticket, out, status);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_set_eb(EbInfo* out, double eb_abs, cudaStream_t s)
-{
-    k_set_eb<<<1, 1, 0, s>>>(out, eb_abs);
+    const uint32_t ctas = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(cdiv(n / 4, 1024), 1), 4864);
+    k_range<<<ctas, 256, 0, s>>>(in, n, mm, mm_next, status);
     return cudaGetLastError();
 }
 
 cudaError_t launch_compress(const CompressArgs& a, cudaStream_t s)
 {
+    // one CTA per 8 shuffle blocks (the tail block included); a CTA is one scan tile
     const uint32_t ctas = (uint32_t)cdiv(a.ntiles, kCompressWarps);
     switch (a.ndim) {
     case 1: k_compress<1><<<ctas, kCompressWarps * 32, 0, s>>>(a); break;

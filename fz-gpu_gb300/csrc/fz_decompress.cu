@@ -28,7 +28,8 @@ __device__ __forceinline__ uint32_t swz_d(uint32_t q)
 __global__ void __launch_bounds__(kDecodeWarps * 32) k_decode(const DecodeArgs a)
 {
     __shared__ __align__(16) uint32_t smem[kDecodeWarps][kBlockWords];
-    __shared__ uint32_t               cta_tile;
+    __shared__ uint32_t               s_cnt[kDecodeWarps];
+    __shared__ uint32_t               cta_tile, s_excl;
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     uint32_t*      sm   = smem[wid];
     if (threadIdx.x == 0) {
@@ -37,30 +38,44 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) k_decode(const DecodeArgs a
         cta_tile = c;
     }
     __syncthreads();
-    const uint32_t t      = cta_tile * kDecodeWarps + wid;
-    const uint32_t ntiles = a.nb + (a.tail ? 1u : 0u);
-    if (t >= ntiles) return;
+    const uint32_t ct = cta_tile;
+    const uint32_t t  = ct * kDecodeWarps + wid;
 
+    uint32_t bm[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cnt = 0;
     if (t < a.nb) {
         const uint4* A4 = reinterpret_cast<const uint4*>(a.st + a.off_a) + 2 * (size_t)t;
-        const uint4  b0 = A4[0], b1 = A4[1];
-        const uint32_t bm[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-        uint32_t       cnt   = 0;
+        const uint4  b0 = __ldg(A4), b1 = __ldg(A4 + 1);
+        bm[0] = b0.x, bm[1] = b0.y, bm[2] = b0.z, bm[3] = b0.w;
+        bm[4] = b1.x, bm[5] = b1.y, bm[6] = b1.z, bm[7] = b1.w;
 #pragma unroll
         for (int i = 0; i < 8; ++i) cnt += __popc(bm[i]);
-        uint32_t excl = 0, povf = 0;
-        if (t == 0) {
-            if (lane == 0) publish(a.state, 0, a.epoch, kFlagIncl, 0, cnt);
+    }
+    // CTA total, then the CTA's first chunk by decoupled look-back
+    if (lane == 0) s_cnt[wid] = cnt;
+    __syncthreads();
+    if (wid == 0) {
+        const uint32_t tot  = __reduce_add_sync(kFull, lane < kDecodeWarps ? s_cnt[lane] : 0u);
+        uint32_t       excl = 0, povf = 0;
+        if (ct == 0) {
+            if (lane == 0) publish(a.state, 0, a.epoch, kFlagIncl, 0, tot);
         } else {
-            if (lane == 0) publish(a.state, t, a.epoch, kFlagAgg, 0, cnt);
-            lookback(a.state, t, a.epoch, a.status, excl, povf);
-            if (lane == 0) publish(a.state, t, a.epoch, kFlagIncl, 0, excl + cnt);
+            if (lane == 0) publish(a.state, ct, a.epoch, kFlagAgg, 0, tot);
+            lookback(a.state, ct, a.epoch, a.status, excl, povf);
+            if (lane == 0) publish(a.state, ct, a.epoch, kFlagIncl, 0, excl + tot);
         }
-        if (t == a.nb - 1 && lane == 0 && excl + cnt != a.nnz) atomicOr(a.status, kStatusCorrupt);
+        if (lane == 0) {
+            s_excl = excl;
+            if (ct == gridDim.x - 1 && excl + tot != a.nnz) atomicOr(a.status, kStatusCorrupt);
+        }
+    }
+    __syncthreads();
+
+    if (t < a.nb) {
+        uint32_t pre = s_excl;
+        for (uint32_t w2 = 0; w2 < wid; ++w2) pre += s_cnt[w2];
         // gather: chunk c = lane + 32 i into the shuffled image S (words 4c..4c+3)
         const uint4*   B   = reinterpret_cast<const uint4*>(a.st + a.off_b);
         const uint32_t lt  = lanemask_lt();
-        uint32_t       pre = excl;
         bool           bad = false;
 #pragma unroll
         for (uint32_t i = 0; i < 8; ++i) {
@@ -89,12 +104,12 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) k_decode(const DecodeArgs a
         uint4* dst = reinterpret_cast<uint4*>(a.codes) + (size_t)t * 256;
 #pragma unroll
         for (uint32_t i = 0; i < 8; ++i) dst[lane + 32 * i] = *reinterpret_cast<const uint4*>(sm + swz_d(lane + 32 * i));
-        return;
+    } else if (t == a.nb && a.tail) {
+        // tail block: raw codes from the sidecar, or zeros without one
+        const uint16_t* src  = a.mode == 1 ? reinterpret_cast<const uint16_t*>(a.st + a.off_c) : nullptr;
+        uint16_t*       dstc = a.codes + (size_t)a.nb * kBlockCodes;
+        for (uint32_t i = lane; i < a.tail; i += 32) dstc[i] = src ? src[i] : (uint16_t)0;
     }
-    // tail block: raw codes from the sidecar, or zeros without one
-    const uint16_t* src  = a.mode == 1 ? reinterpret_cast<const uint16_t*>(a.st + a.off_c) : nullptr;
-    uint16_t*       dstc = a.codes + (size_t)a.nb * kBlockCodes;
-    for (uint32_t i = lane; i < a.tail; i += 32) dstc[i] = src ? src[i] : (uint16_t)0;
 }
 
 cudaError_t launch_decode(const DecodeArgs& a, cudaStream_t s)

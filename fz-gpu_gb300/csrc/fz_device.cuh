@@ -26,6 +26,17 @@ struct EbInfo {
     uint32_t nonfinite;
 };
 
+// Order-preserving u32 encoding of a (non-NaN) float, for atomicMin/atomicMax.
+__device__ __forceinline__ uint32_t f2ord(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t o)
+{
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o);
+}
+
 // ------------------------------------------------------------ status bits --
 constexpr uint32_t kStatusTimeout   = 1u;
 constexpr uint32_t kStatusNonfinite = 2u;
@@ -52,8 +63,16 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f)
 }
 
 // ------------------------------------------------------------ prequant --
-// round(x * ebx2_r) in float, ties away from zero (lorenzo_var.cuh:81,125,265).
-__device__ __forceinline__ float pq(float v, float r) { return roundf(__fmul_rn(v, r)); }
+// Round half away from zero as trunc(v + copysign(pred(1/2), v)), pred(1/2) the float
+// just below 1/2: with round-to-nearest addition this equals round(v) for every float
+// (checked exhaustively over all finite floats; +-Inf and NaN pass through).
+__device__ __forceinline__ float round_half_away(float v)
+{
+    const float h = __uint_as_float((__float_as_uint(v) & 0x80000000u) | 0x3EFFFFFFu);
+    return truncf(__fadd_rn(v, h));
+}
+// Prequantisation round(x * ebx2_r) in float (lorenzo_var.cuh:81,125,265).
+__device__ __forceinline__ float pq(float v, float r) { return round_half_away(__fmul_rn(v, r)); }
 
 // (u16)fabs(d) | (d < 0) << 15 -- the expression of lorenzo_var.cuh:169-171.
 __device__ __forceinline__ uint32_t pack_signed(float d)
@@ -112,40 +131,49 @@ __device__ __forceinline__ uint64_t state_pack(uint32_t epoch, uint64_t flag, ui
 {
     return ((uint64_t)epoch << 36) | (flag << 34) | ((uint64_t)(ovf & 1u) << 32) | value;
 }
-__device__ __forceinline__ void st_release(uint64_t* p, uint64_t v)
+// The value and its flag share one 64-bit word, so relaxed GPU-scope accesses suffice:
+// no other memory is published through it.
+__device__ __forceinline__ void st_state(uint64_t* p, uint64_t v)
 {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
-__device__ __forceinline__ uint64_t ld_acquire(const uint64_t* p)
+__device__ __forceinline__ uint64_t ld_state(const uint64_t* p)
 {
     uint64_t v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
 
 constexpr uint32_t kSpinLimit = 1u << 22;  // polls before a wait gives up (~0.3 s)
 
 // Warp-cooperative decoupled look-back (single pass, Merrill & Garland 2016).
-// Tile `t` has published its aggregate already (unless t == 0).  Lane l inspects tile
-// t-1-l-32k.  Returns the exclusive prefix (value) and OR of the ovf bits of all
-// predecessors; every lane gets the result.  On a wait that exceeds kSpinLimit polls
-// the status word gets kStatusTimeout and the missing tiles count as 0, so no warp
-// ever waits forever.
+// Tile `t` has published its aggregate already (unless t == 0).  Each round the warp
+// inspects a window of 128 predecessors -- lane l loads tiles t-1-4l .. t-4-4l -- so a
+// tile started next to a thousand others still finds an inclusive prefix in a few
+// rounds.  Returns the exclusive prefix (value) and the OR of the predecessors' ovf
+// bits in every lane.  A wait longer than kSpinLimit polls raises kStatusTimeout and
+// counts the missing tiles as 0, so no warp ever waits forever.
 __device__ __forceinline__ void lookback(const uint64_t* state, uint32_t t, uint32_t epoch,
                                          uint32_t* status, uint32_t& excl, uint32_t& ovf)
 {
     const uint32_t lane = threadIdx.x & 31;
     uint32_t       acc = 0, acc_ovf = 0;
-    int64_t        pos   = (int64_t)t - 1 - lane;
-    uint32_t       spins = 0;
+    int64_t        base    = (int64_t)t - 1 - 4 * (int64_t)lane;
+    uint32_t       spins   = 0;
     bool           gave_up = false;
     while (true) {
-        uint64_t s;
-        bool     ready;
+        uint64_t s[4];
+        bool     ready[4];
         while (true) {
-            s     = pos >= 0 ? ld_acquire(state + pos) : state_pack(epoch, kFlagIncl, 0, 0);
-            ready = (uint32_t)(s >> 36) == epoch && ((s >> 34) & 3u) != 0;
-            if (__all_sync(kFull, ready)) break;
+            bool all = true;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int64_t pos = base - j;
+                s[j]     = pos >= 0 ? ld_state(state + pos) : state_pack(epoch, kFlagIncl, 0, 0);
+                ready[j] = (uint32_t)(s[j] >> 36) == epoch && ((s[j] >> 34) & 3u) != 0;
+                all      = all && ready[j];
+            }
+            if (__all_sync(kFull, all)) break;
             if (++spins > kSpinLimit) {
                 gave_up = true;
                 break;
@@ -154,22 +182,26 @@ __device__ __forceinline__ void lookback(const uint64_t* state, uint32_t t, uint
         }
         if (gave_up) {
             if (lane == 0) atomicOr(status, kStatusTimeout);
-            // not-ready tiles count as an inclusive 0 so the chain terminates here
-            if (!ready) s = state_pack(epoch, kFlagIncl, 0, 0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)  // not-ready tiles end the walk as an inclusive 0
+                if (!ready[j]) s[j] = state_pack(epoch, kFlagIncl, 0, 0);
         }
-        const uint32_t flag  = (uint32_t)(s >> 34) & 3u;
-        const uint32_t incl  = __ballot_sync(kFull, flag == kFlagIncl);
-        const uint32_t val   = (uint32_t)s;
-        const uint32_t ovbit = (uint32_t)(s >> 32) & 1u;
-        if (incl) {
-            const uint32_t k = __ffs(incl) - 1;  // nearest predecessor holding a prefix
-            acc += __reduce_add_sync(kFull, lane <= k ? val : 0u);
-            acc_ovf |= __reduce_or_sync(kFull, lane <= k ? ovbit : 0u);
-            break;
-        }
-        acc += __reduce_add_sync(kFull, val);
-        acc_ovf |= __reduce_or_sync(kFull, ovbit);
-        pos -= 32;
+        uint32_t mine = 0;  // bit j: tile base-j holds an inclusive prefix
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mine |= (((s[j] >> 34) & 3u) == kFlagIncl) ? (1u << j) : 0u;
+        const uint32_t any = __ballot_sync(kFull, mine != 0);
+        // lanes before the first lane holding a prefix take all 4 tiles; that lane
+        // takes its tiles up to its first prefix; later lanes take none
+        const int first = any ? __ffs(any) - 1 : 32;
+        const int jmax  = (int)lane < first ? 3 : ((int)lane == first ? __ffs(mine) - 1 : -1);
+        uint32_t  v = 0, o = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (j <= jmax) v += (uint32_t)s[j], o |= (uint32_t)(s[j] >> 32) & 1u;
+        acc += __reduce_add_sync(kFull, v);
+        acc_ovf |= __reduce_or_sync(kFull, o);
+        if (any) break;
+        base -= 128;
     }
     excl = acc;
     ovf  = acc_ovf;
@@ -179,7 +211,7 @@ __device__ __forceinline__ void lookback(const uint64_t* state, uint32_t t, uint
 __device__ __forceinline__ void publish(uint64_t* state, uint32_t t, uint32_t epoch,
                                         uint64_t flag, uint32_t ovf, uint32_t value)
 {
-    st_release(state + t, state_pack(epoch, flag, ovf, value));
+    st_state(state + t, state_pack(epoch, flag, ovf, value));
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt()

@@ -32,8 +32,9 @@ struct CompressArgs {
     uint32_t     al_x, al_xy, al_xyx;  // 1 when the halo row offsets are multiples of 4
     uint32_t     nb, ntiles, nwords, mode, ndim, sidecar_bytes;
     uint64_t     off_a, off_c, off_b, off_sign;
-    const EbInfo* eb;   // device constants from the range pass (relative eb), or null
-    EbInfo       ebh;   // constants computed on the host (absolute eb)
+    const uint32_t* mm;  // range-pass accumulators (relative eb), or null
+    double       eb_rel; // relative error bound (with mm)
+    EbInfo       ebh;    // constants computed on the host (absolute eb)
     uint64_t*    state;
     uint32_t*    ticket;
     uint32_t*    status;
@@ -61,9 +62,8 @@ struct ReconArgs {
 };
 
 // launchers (return the launch error)
-cudaError_t launch_range(const float* in, uint32_t n, double eb, int rel, float2* partials,
-                         uint32_t* ticket, EbInfo* out, uint32_t* status, cudaStream_t s);
-cudaError_t launch_set_eb(EbInfo* out, double eb_abs, cudaStream_t s);
+cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* mm_next,
+                         uint32_t* status, cudaStream_t s);
 cudaError_t launch_compress(const CompressArgs& a, cudaStream_t s);
 cudaError_t launch_decode(const DecodeArgs& a, cudaStream_t s);
 cudaError_t launch_reconstruct(const ReconArgs& a, cudaStream_t s);
@@ -80,6 +80,5 @@ cudaError_t launch_scan_encode(const uint8_t* shuffled, const uint32_t* byteflag
                                uint64_t* state, uint32_t* ticket, uint32_t* status,
                                uint32_t* total, uint32_t epoch, cudaStream_t s);
 
-constexpr int kRangeGrid = 608;  // 4 CTAs per SM on 152 SMs
 
 }  // namespace fz
