@@ -55,6 +55,15 @@ class Header(C.Structure):
 
 assert C.sizeof(Header) == HEADER_BYTES
 
+
+class Field(C.Structure):
+    _fields_ = [("src", C.c_void_p), ("dst", C.c_void_p), ("n", C.c_uint64), ("dims", Dims),
+                ("eb", C.c_double), ("dst_capacity", C.c_uint64), ("src_bytes", C.c_uint64),
+                ("header", Header)]
+
+
+COMPRESS, DECOMPRESS = 0, 1
+
 _lock = threading.Lock()
 _lib = None
 
@@ -84,6 +93,11 @@ SIGNATURES = {
     "fz_lorenzo_reconstruct": (_I, [_P, _P, _P, Dims, _D, _P]),
     "fz_bitshuffle_flag": (_I, [_P, _P, _U64, _P, _P, _P]),
     "fz_scan_encode": (_I, [_P, _P, _P, _U64, _P, _P, _PU64, _P]),
+    "fz_compress_batch": (_I, [_P, _P, _U32, _I, _I, _P]),
+    "fz_decompress_batch": (_I, [_P, _P, _U32, _P]),
+    "fz_batch_create": (_I, [_P, _P, _U32, _I, _I, _I, C.POINTER(_P)]),
+    "fz_batch_launch": (_I, [_P, _P]),
+    "fz_batch_destroy": (_I, [_P]),
 }
 
 
@@ -189,7 +203,7 @@ class Workspace:
         """Status of a look-back that waits on a tile nothing publishes (FZ_TIMEOUT)."""
         return lib().fz_selftest_wait_timeout(self.handle, _stream_handle(stream))
 
-    KERNELS = ("k_range", "k_compress", "k_decode", "k_recon")
+    KERNELS = ("k_range", "k_compress", "k_offsets", "k_decode", "k_recon")
 
     def enable_timing(self, capacity):
         _check("fz_workspace_enable_timing", lib().fz_workspace_enable_timing(self.handle, int(capacity)))
@@ -339,3 +353,55 @@ def scan_encode(shuffled, byteflag, n_codes, ws=None, stream=None):
                               C.byref(nnz), _stream_handle(stream))
     _check("fz_scan_encode", st)
     return pre, out[: 16 * nnz.value], nnz.value
+
+
+# ------------------------------------------------------------------ batches
+def fields_array(items):
+    """ctypes array of Field from dicts with the struct's keys."""
+    arr = (Field * len(items))()
+    for i, it in enumerate(items):
+        f = arr[i]
+        f.src = it.get("src")
+        f.dst = it.get("dst")
+        f.n = int(it.get("n", 0))
+        f.dims = _dims(it.get("dims", (1, 1, 1)))
+        f.eb = float(it.get("eb", 0.0))
+        f.dst_capacity = int(it.get("dst_capacity", 0))
+        f.src_bytes = int(it.get("src_bytes", 0))
+        if it.get("header") is not None:
+            f.header = it["header"]
+    return arr
+
+
+def compress_batch(ws, fields, rel=True, mode=MODE_SIDECAR, stream=None):
+    _check("fz_compress_batch", lib().fz_compress_batch(ws.handle, fields, len(fields), EB_REL if rel else EB_ABS,
+                                                        mode, _stream_handle(stream)))
+
+
+def decompress_batch(ws, fields, stream=None):
+    _check("fz_decompress_batch", lib().fz_decompress_batch(ws.handle, fields, len(fields), _stream_handle(stream)))
+
+
+class Batch:
+    """A batch recorded once into a CUDA graph (fz_batch_create) and replayed."""
+
+    def __init__(self, ws, fields, direction, rel=True, mode=MODE_SIDECAR):
+        self.ws, self.fields = ws, fields  # keep the buffers' owners alive
+        h = C.c_void_p()
+        _check("fz_batch_create", lib().fz_batch_create(ws.handle, fields, len(fields), direction,
+                                                        EB_REL if rel else EB_ABS, mode, C.byref(h)))
+        self.handle = h
+
+    def launch(self, stream=None):
+        _check("fz_batch_launch", lib().fz_batch_launch(self.handle, _stream_handle(stream)))
+
+    def close(self):
+        if self.handle:
+            lib().fz_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -29,11 +29,14 @@ Layout make_layout(uint64_t n, uint32_t x, uint32_t y, uint32_t z, uint32_t mode
     L.off_c  = L.off_a + pad16(4ull * L.nwords);
     uint64_t sc = 0;
     if (mode == FZ_MODE_SIDECAR) {
+        // Section C: raw tail codes | 1D sign bits | chunk offset of every shuffle block
         sc += pad16(2ull * L.tail);
         L.off_sign = L.off_c + sc;
         if (L.ndim == 1) sc += pad16(4 * cdiv(n, 32));
+        L.off_boff = L.off_c + sc;
+        sc += pad16(4ull * (L.nb + 1));
     } else {
-        L.off_sign = L.off_c;
+        L.off_sign = L.off_boff = L.off_c;
     }
     L.sidecar_bytes = (uint32_t)sc;
     L.off_b         = L.off_c + sc;
@@ -49,13 +52,13 @@ struct fz_workspace {
     void*     d_base;
     size_t    d_bytes;
     uint64_t* state;
-    uint32_t* tickets;  // [0] compress, [1] decode, [2] scan-encode, [3] range
+    uint32_t* tickets;  // [0] compress, [1] offsets, [2] scan-encode
     uint32_t* status;
     uint32_t* total;
-    uint32_t* mm;       // two range accumulator pairs (min, max as ordered u32)
-    uint32_t  range_calls;
+    uint32_t* epoch;    // device epoch of the scan state
+    uint32_t* mm;       // range accumulators (min, max as ordered u32)
     uint16_t* codes;
-    uint32_t  epoch;
+    uint32_t* boff;     // chunk offset of each shuffle block (decompression)
     uint8_t*  h_pinned;  // 64-byte header + status word
     // host-buffer path staging, allocated on first use
     float*    d_field;
@@ -93,17 +96,6 @@ fz_status check_dims(uint64_t n, fz_dims d)
 }
 
 uint64_t max_stream(const Layout& L) { return L.off_b + 16ull * kChunks * L.nb; }
-
-uint32_t next_epoch(fz_workspace* ws, cudaStream_t s)
-{
-    ws->epoch++;
-    if (ws->epoch >= (1u << 28)) {
-        // the 28-bit epoch tag wraps: clear the tile states once
-        cudaMemsetAsync(ws->state, 0, (size_t)ws->max_tiles * 8, s);
-        ws->epoch = 1;
-    }
-    return ws->epoch;
-}
 
 // Brackets one kernel launch with a pair of events when timing is enabled.
 struct KernelTimer {
@@ -246,6 +238,7 @@ fz_status fz_workspace_bytes(uint64_t max_n, uint64_t* bytes)
     b += 64;                        // tickets, status, total
     b += 16;                        // range accumulators
     b += pad16(2 * max_n + 16);     // decode scratch
+    b += pad16(4 * tiles + 4);      // block offsets
     *bytes = b;
     return FZ_SUCCESS;
 }
@@ -274,12 +267,14 @@ fz_status fz_workspace_create(uint64_t max_n, fz_workspace** out)
     ws->tickets = reinterpret_cast<uint32_t*>(p);
     ws->status  = ws->tickets + 4;
     ws->total   = ws->tickets + 5;
+    ws->epoch   = ws->tickets + 6;
     p += 64;
     ws->mm       = reinterpret_cast<uint32_t*>(p), p += 16;
-    ws->codes    = reinterpret_cast<uint16_t*>(p);
+    ws->codes    = reinterpret_cast<uint16_t*>(p), p += pad16(2 * max_n + 16);
+    ws->boff     = reinterpret_cast<uint32_t*>(p);
     e            = cudaMemset(ws->d_base, 0, bytes);
     if (e == cudaSuccess) {
-        const uint32_t init[4] = {0xFFFFFFFFu, 0u, 0xFFFFFFFFu, 0u};  // empty min/max
+        const uint32_t init[2] = {0xFFFFFFFFu, 0u};  // empty min/max
         e                      = cudaMemcpy(ws->mm, init, sizeof(init), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = cudaMallocHost((void**)&ws->h_pinned, 128);
@@ -288,8 +283,7 @@ fz_status fz_workspace_create(uint64_t max_n, fz_workspace** out)
         delete ws;
         return map_err(e, FZ_FAIL_GPU_MALLOC);
     }
-    ws->epoch = 0;
-    *out      = ws;
+    *out = ws;
     return FZ_SUCCESS;
 }
 
@@ -386,16 +380,15 @@ fz_status fz_compress(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims d
     a.al_x = (L.x % 4) == 0, a.al_xy = (L.xy % 4) == 0, a.al_xyx = ((L.xy + L.x) % 4) == 0;
     a.nb = L.nb, a.ntiles = L.nb + (L.tail ? 1 : 0), a.nwords = L.nwords;
     a.mode = mode, a.ndim = L.ndim, a.sidecar_bytes = L.sidecar_bytes;
-    a.off_a = L.off_a, a.off_c = L.off_c, a.off_b = L.off_b, a.off_sign = L.off_sign;
-    a.state = ws->state, a.ticket = ws->tickets + 0, a.status = ws->status;
-    a.epoch = next_epoch(ws, s);
+    a.off_a = L.off_a, a.off_c = L.off_c, a.off_b = L.off_b, a.off_sign = L.off_sign, a.off_boff = L.off_boff;
+    a.state = ws->state, a.ticket = ws->tickets + 0, a.status = ws->status, a.epoch = ws->epoch;
+    a.boff  = mode == FZ_MODE_SIDECAR ? reinterpret_cast<uint32_t*>(a.out + L.off_boff) : nullptr;
     cudaError_t e = cudaSuccess;
     if (eb_mode == FZ_EB_REL) {
-        KernelTimer     t(ws, s, 0);
-        const uint32_t  slot = (ws->range_calls++) & 1u;
-        e                    = launch_range(d_in, L.n, ws->mm + 2 * slot, ws->mm + 2 * (slot ^ 1u), ws->status, s);
-        a.mm                 = ws->mm + 2 * slot;
-        a.eb_rel             = eb;
+        KernelTimer t(ws, s, 0);
+        e        = launch_range(d_in, L.n, ws->mm, ws->status, s);
+        a.mm     = ws->mm;
+        a.eb_rel = eb;
     } else {
         a.mm            = nullptr;
         a.ebh.eb_abs    = eb;
@@ -442,29 +435,49 @@ fz_status fz_decompress(fz_workspace* ws, const void* d_stream, uint64_t stream_
     if (h.n > out_capacity_elems || h.n > ws->max_n) return FZ_OUT_OF_SPACE;
 
     DecodeArgs d{};
-    d.st = static_cast<const uint8_t*>(d_stream);
+    d.st    = static_cast<const uint8_t*>(d_stream);
     d.codes = ws->codes;
-    d.n = L.n, d.nb = L.nb, d.tail = L.tail, d.mode = L.mode;
-    d.off_a = L.off_a, d.off_c = L.off_c, d.off_b = L.off_b, d.nnz = h.nnz;
-    d.state = ws->state, d.ticket = ws->tickets + 1, d.status = ws->status;
-    d.epoch = next_epoch(ws, s);
-    cudaError_t e;
-    {
+    d.boff  = ws->boff;
+    d.out   = d_out;
+    d.n = L.n, d.nl = L.nl, d.x = L.x, d.y = L.y, d.z = L.z;
+    d.nb = L.nb, d.tail = L.tail, d.mode = L.mode, d.nwords = L.nwords;
+    d.off_a = L.off_a, d.off_c = L.off_c, d.off_b = L.off_b, d.off_sign = L.off_sign, d.nnz = h.nnz;
+    d.off_boff = L.off_boff;
+    d.ebx2     = h.ebx2;
+    d.status   = ws->status;
+    cudaError_t e = cudaSuccess;
+    if (L.mode == FZ_MODE_SIDECAR) {
+        d.boff = reinterpret_cast<const uint32_t*>(d.st + L.off_boff);  // written by the compressor
+    } else {
         KernelTimer t(ws, s, 2);
-        e = launch_decode(d, s);
+        e = launch_offsets(d.st, L.off_a, L.nb, L.nwords, h.nnz, ws->boff, ws->state, ws->tickets + 1,
+                           ws->status, ws->epoch, s);
     }
     if (e != cudaSuccess) return map_err(e);
-    ReconArgs r{};
-    r.codes    = ws->codes;
-    r.signbits = (L.ndim == 1 && L.mode == FZ_MODE_SIDECAR)
-                     ? reinterpret_cast<const uint32_t*>(d.st + L.off_sign) : nullptr;
-    r.signum = nullptr;
-    r.out    = d_out;
-    r.n = L.n, r.nl = L.nl, r.x = L.x, r.y = L.y, r.z = L.z;
-    r.ebx2 = h.ebx2;
     {
         KernelTimer t(ws, s, 3);
+        e = launch_decompress_fused(d, s);
+    }
+    if (e == cudaErrorNotSupported) {
+        // two-pass shapes (3D, rows not a multiple of 4): codes to scratch, then x_lorenzo
+        (void)cudaGetLastError();
+        {
+            KernelTimer t(ws, s, 3);
+            e = launch_decode(d, s);
+        }
+        if (e != cudaSuccess) return map_err(e);
+        ReconArgs r{};
+        r.codes    = ws->codes;
+        r.signbits = (L.ndim == 1 && L.mode == FZ_MODE_SIDECAR)
+                         ? reinterpret_cast<const uint32_t*>(d.st + L.off_sign) : nullptr;
+        r.signum = nullptr;
+        r.out    = d_out;
+        r.n = L.n, r.nl = L.nl, r.x = L.x, r.y = L.y, r.z = L.z;
+        r.ebx2 = h.ebx2;
+        KernelTimer t(ws, s, 4);
         e = launch_reconstruct(r, s);
+    } else if (e == cudaSuccess && L.n > L.nl) {
+        e = launch_zero_tail(d_out, L.nl, L.n, s);
     }
     return map_err(e);
 }
@@ -545,9 +558,8 @@ fz_status fz_selftest_wait_timeout(fz_workspace* ws, fz_stream_t stream)
     fz_status st = check_device(ws);
     if (st != FZ_SUCCESS) return st;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    // a fresh epoch: tile 0 holds a word of an older epoch, which reads as "not ready"
-    const uint32_t e = next_epoch(ws, s);
-    cudaError_t    r = launch_wait_selftest(ws->state, e, ws->status, s);
+    // the device epoch is one no launch has used yet: tile 0 never reads as ready
+    cudaError_t r = launch_wait_selftest(ws->state, ws->epoch, ws->status, s);
     if (r != cudaSuccess) return map_err(r);
     return fz_workspace_status(ws, stream);
 }
@@ -598,7 +610,7 @@ fz_status fz_scan_encode(fz_workspace* ws, const uint8_t* d_shuffled, const uint
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     cudaError_t  e = launch_scan_encode(d_shuffled, d_byteflag, (uint32_t)n_codes, d_presum, d_out,
                                         ws->state, ws->tickets + 2, ws->status, ws->total,
-                                        next_epoch(ws, s), s);
+                                        ws->epoch, s);
     if (e != cudaSuccess) return map_err(e);
     if (nnz) {
         e = cudaMemcpyAsync(ws->h_pinned, ws->total, 4, cudaMemcpyDeviceToHost, s);
@@ -609,6 +621,96 @@ fz_status fz_scan_encode(fz_workspace* ws, const uint8_t* d_shuffled, const uint
         *nnz = t;
         return fz_workspace_status(ws, stream);
     }
+    return FZ_SUCCESS;
+}
+
+// ----------------------------------------------------------------- batching --
+fz_status fz_compress_batch(fz_workspace* ws, const fz_field* fields, uint32_t count, fz_eb_mode eb_mode,
+                            fz_mode mode, fz_stream_t stream)
+{
+    if (!ws || (!fields && count)) return FZ_INVALID_ARG;
+    for (uint32_t i = 0; i < count; ++i) {
+        const fz_field& f = fields[i];
+        fz_status st = fz_compress(ws, static_cast<const float*>(f.src), f.n, f.dims, f.eb, eb_mode, mode,
+                                   f.dst, f.dst_capacity, nullptr, stream);
+        if (st != FZ_SUCCESS) return st;
+    }
+    return FZ_SUCCESS;
+}
+
+fz_status fz_decompress_batch(fz_workspace* ws, const fz_field* fields, uint32_t count, fz_stream_t stream)
+{
+    if (!ws || (!fields && count)) return FZ_INVALID_ARG;
+    for (uint32_t i = 0; i < count; ++i) {
+        const fz_field& f = fields[i];
+        fz_status st = fz_decompress(ws, f.src, f.src_bytes, &f.header, static_cast<float*>(f.dst),
+                                     f.dst_capacity, stream);
+        if (st != FZ_SUCCESS) return st;
+    }
+    return FZ_SUCCESS;
+}
+
+}  // extern "C"
+
+struct fz_batch {
+    cudaGraph_t     graph = nullptr;
+    cudaGraphExec_t exec  = nullptr;
+};
+
+extern "C" {
+
+fz_status fz_batch_create(fz_workspace* ws, const fz_field* fields, uint32_t count, fz_direction dir,
+                          fz_eb_mode eb_mode, fz_mode mode, fz_batch** out)
+{
+    if (!ws || !out || (!fields && count) || (dir != FZ_COMPRESS && dir != FZ_DECOMPRESS)) return FZ_INVALID_ARG;
+    *out = nullptr;
+    cudaStream_t cs;
+    cudaError_t  e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return map_err(e);
+    // no timing events inside a graph
+    const uint32_t tcap = ws->tcap;
+    ws->tcap            = 0;
+    fz_batch* b         = new (std::nothrow) fz_batch();
+    fz_status st        = b ? FZ_SUCCESS : FZ_FAIL_GPU_MALLOC;
+    if (st == FZ_SUCCESS) {
+        e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) st = map_err(e);
+    }
+    if (st == FZ_SUCCESS) {
+        fz_stream_t h = reinterpret_cast<fz_stream_t>(cs);
+        st = dir == FZ_COMPRESS ? fz_compress_batch(ws, fields, count, eb_mode, mode, h)
+                                : fz_decompress_batch(ws, fields, count, h);
+        cudaGraph_t g = nullptr;
+        e             = cudaStreamEndCapture(cs, &g);
+        if (st == FZ_SUCCESS && e != cudaSuccess) st = map_err(e);
+        b->graph = g;
+        if (st == FZ_SUCCESS) {
+            e = cudaGraphInstantiate(&b->exec, g, 0);
+            if (e != cudaSuccess) st = map_err(e);
+        }
+    }
+    ws->tcap = tcap;
+    cudaStreamDestroy(cs);
+    if (st != FZ_SUCCESS) {
+        fz_batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_batch_launch(fz_batch* b, fz_stream_t stream)
+{
+    if (!b || !b->exec) return FZ_INVALID_ARG;
+    return map_err(cudaGraphLaunch(b->exec, reinterpret_cast<cudaStream_t>(stream)));
+}
+
+fz_status fz_batch_destroy(fz_batch* b)
+{
+    if (!b) return FZ_INVALID_ARG;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    delete b;
     return FZ_SUCCESS;
 }
 

@@ -239,26 +239,27 @@ __device__ __forceinline__ void codes4(const float* __restrict__ in, const Geo& 
 }
 
 // --------------------------------------------------------------- range --
+constexpr int kRangeUnroll = 8;
 // max and min of the field (fz.cu:137) as order-preserving integers folded with one
-// atomicMin/atomicMax per CTA into mm[0..1].  The other accumulator pair (used by the
-// previous call) is reset here for the next one.  Four 16-byte loads in flight per
-// thread; NaN/Inf raise kStatusNonfinite.
+// atomicMin/atomicMax per CTA into mm[0..1], which the consuming compress kernel resets
+// to "empty" for the next call.  kRangeUnroll 16-byte loads in flight per thread;
+// NaN/Inf raise kStatusNonfinite.
 __global__ void __launch_bounds__(256) k_range(const float* __restrict__ in, uint32_t n, uint32_t* mm,
-                                               uint32_t* mm_next, uint32_t* status)
+                                               uint32_t* status)
 {
     __shared__ uint32_t smn[8], smx[8], snf[8];
-    if (blockIdx.x == 0 && threadIdx.x == 0) mm_next[0] = 0xFFFFFFFFu, mm_next[1] = 0u;
     float          mn = INFINITY, mx = -INFINITY;
     uint32_t       nonfinite = 0;
     const uint32_t n4        = n / 4;
-    const uint32_t per       = blockDim.x * 4;
+    const uint32_t per       = blockDim.x * kRangeUnroll;
+    // one resident wave; each pass keeps kRangeUnroll 16-byte loads in flight per thread
     for (uint32_t b = blockIdx.x * per + threadIdx.x; b < n4; b += gridDim.x * per) {
-        float4 v[4];
+        float4 v[kRangeUnroll];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < kRangeUnroll; ++k)
             if (b + k * blockDim.x < n4) v[k] = ldg4(in + 4 * (size_t)(b + k * blockDim.x));
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < kRangeUnroll; ++k) {
             if (b + k * blockDim.x >= n4) continue;
             mn = fminf(fminf(mn, v[k].x), fminf(v[k].y, fminf(v[k].z, v[k].w)));
             mx = fmaxf(fmaxf(mx, v[k].x), fmaxf(v[k].y, fmaxf(v[k].z, v[k].w)));
@@ -334,181 +335,225 @@ __device__ __forceinline__ uint32_t swz(uint32_t q)
     return ((g << 3) | (t ^ (g & 7u))) << 2;
 }
 
+// Persistent: one resident wave of CTAs; each CTA repeatedly takes the next scan tile
+// (8 shuffle blocks, one per warp) from the ticket counter.  Tickets are handed out in
+// order, so every predecessor of a tile has been taken by a running CTA and the
+// look-back always makes progress.  The last of the nctiles + gridDim.x fetches resets
+// the counter for the next call.
 template <int ND>
 __global__ void __launch_bounds__(kCompressWarps * 32) k_compress(const CompressArgs a)
 {
     __shared__ __align__(16) uint32_t smem[kCompressWarps][kBlockWords];
     __shared__ uint32_t               s_cnt[kCompressWarps], s_ovf[kCompressWarps];
-    __shared__ uint32_t               cta_tile, s_excl;
+    __shared__ uint32_t               cta_tile, s_excl, s_epoch;
     __shared__ EbInfo                 s_eb;
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     uint32_t*      sm   = smem[wid];
+    const uint32_t nct  = (uint32_t)cdiv(a.ntiles, kCompressWarps);
 
-    // Scan tiles are CTAs (8 shuffle blocks), handed out in launch order so that every
-    // predecessor of a tile has started: the look-back always makes progress.
     if (threadIdx.x == 0) {
-        const uint32_t c = atomicAdd(a.ticket, 1u);
-        if (c == gridDim.x - 1) atomicExch(a.ticket, 0u);  // last ticket: reset for the next call
-        cta_tile = c;
-        s_eb     = a.mm ? eb_from_range(ord2f(__ldcg(a.mm)), ord2f(__ldcg(a.mm + 1)), a.eb_rel) : a.ebh;
+        s_eb    = a.mm ? eb_from_range(ord2f(__ldcg(a.mm)), ord2f(__ldcg(a.mm + 1)), a.eb_rel) : a.ebh;
+        s_epoch = __ldcg(a.epoch);
+        __threadfence();  // both reads complete before the first ticket (the last one resets them)
     }
-    __syncthreads();
-    const uint32_t ct = cta_tile;
-    const uint32_t t  = ct * kCompressWarps + wid;  // this warp's shuffle block
-
-    const EbInfo eb = s_eb;
-    const float  r  = eb.ebx2_r;
-    Geo          g;
+    Geo g;
     g.nl = a.nl, g.x = a.x, g.y = a.y, g.xy = a.xy, g.lim = a.n;
     g.dx = a.dx, g.dxy = a.dxy, g.al_x = a.al_x, g.al_xy = a.al_xy, g.al_xyx = a.al_xyx;
+    uint32_t* signw = (ND == 1 && a.mode == 1) ? reinterpret_cast<uint32_t*>(a.out + a.off_sign) : nullptr;
 
-    const uint32_t base  = t * kBlockCodes;
-    uint32_t       ovf   = 0, cnt = 0;
-    uint32_t       bm[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    uint32_t*      signw = (ND == 1 && a.mode == 1) ? reinterpret_cast<uint32_t*>(a.out + a.off_sign) : nullptr;
+    while (true) {
+        if (threadIdx.x == 0) {
+            const Ticket tk = take_ticket(a.ticket, a.epoch, nct + gridDim.x);
+            if (tk.last && a.mm) a.mm[0] = 0xFFFFFFFFu, a.mm[1] = 0u;  // empty range for the next call
+            cta_tile = tk.tile;
+        }
+        __syncthreads();
+        const uint32_t ct    = cta_tile;
+        const uint32_t epoch = s_epoch;
+        if (ct >= nct) break;  // uniform
+        const EbInfo   eb   = s_eb;
+        const float    r    = eb.ebx2_r;
+        const uint32_t t    = ct * kCompressWarps + wid;  // this warp's shuffle block
+        const uint32_t base = t * kBlockCodes;
+        uint32_t       ovf  = 0, cnt = 0;
+        uint32_t       bm[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
-    if (t < a.nb) {
-        // ---- phase A: codes of the block into shared memory (swizzled) ----
+        if (t < a.nb) {
+            // ---- phase A: codes of the block into shared memory (swizzled) ----
 #pragma unroll 2
-        for (uint32_t it = 0; it < 16; ++it) {
-            const uint32_t e0 = base + it * 128 + lane * 4;
-            uint32_t       c[4], sgn = 0;
-            codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
-            const uint32_t q = it * 16 + (lane >> 1);
-            *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
-                make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+            for (uint32_t it = 0; it < 16; ++it) {
+                const uint32_t e0 = base + it * 128 + lane * 4;
+                uint32_t       c[4], sgn = 0;
+                codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
+                const uint32_t q = it * 16 + (lane >> 1);
+                *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
+                    make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+                if (ND == 1 && signw) {
+                    // 4 sign bits per lane -> one u32 per 8 lanes (32 consecutive elements)
+                    uint32_t v = sgn << ((lane & 7u) * 4);
+                    v |= __shfl_xor_sync(kFull, v, 1);
+                    v |= __shfl_xor_sync(kFull, v, 2);
+                    v |= __shfl_xor_sync(kFull, v, 4);
+                    if ((lane & 7u) == 0) signw[(base >> 5) + it * 4 + (lane >> 3)] = v;
+                }
+            }
+            __syncwarp();
+            // ---- phase B: lane g transposes group g (words g*32 .. g*32+31) ----
+            uint32_t w[32];
+#pragma unroll
+            for (uint32_t tt = 0; tt < 8; ++tt) {
+                const uint4 v = *reinterpret_cast<const uint4*>(sm + swz(lane * 8 + tt));
+                w[4 * tt] = v.x, w[4 * tt + 1] = v.y, w[4 * tt + 2] = v.z, w[4 * tt + 3] = v.w;
+            }
+            transpose32(w);
+            __syncwarp();
+            // shuffled image S[p*32 + g] = w[p] (bitshuffleAndBitflag's out, fz.cu:82)
+#pragma unroll
+            for (uint32_t p = 0; p < 32; ++p) sm[p * 32 + lane] = w[p];
+            __syncwarp();
+            // ---- phase C: chunk c = lane + 32 i; ballot i is bitmap word 8t+i ----
+#pragma unroll
+            for (uint32_t i = 0; i < 8; ++i) {
+                const uint4 v = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
+                bm[i] = __ballot_sync(kFull, (v.x | v.y | v.z | v.w) != 0);
+                cnt += __popc(bm[i]);
+            }
+            if (lane == 0) {
+                uint4* A = reinterpret_cast<uint4*>(a.out + a.off_a) + 2 * (size_t)t;
+                A[0]     = make_uint4(bm[0], bm[1], bm[2], bm[3]);
+                A[1]     = make_uint4(bm[4], bm[5], bm[6], bm[7]);
+            }
+        } else if (t == a.nb && a.n > base) {
+            // ---- tail block: n mod 2048 codes, never shuffled (fz.cu:173) ----
+            const uint32_t tail = a.n - base;
+            uint16_t*      tc   = (a.mode == 1) ? reinterpret_cast<uint16_t*>(a.out + a.off_c) : nullptr;
+            for (uint32_t it = 0; it * 128 < tail; ++it) {
+                const uint32_t e0 = base + it * 128 + lane * 4;
+                uint32_t       c[4], sgn = 0;
+                codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (tc && e0 + j < a.n) tc[e0 + j - base] = (uint16_t)c[j];
+                if (ND == 1 && signw) {
+                    uint32_t v = sgn << ((lane & 7u) * 4);
+                    v |= __shfl_xor_sync(kFull, v, 1);
+                    v |= __shfl_xor_sync(kFull, v, 2);
+                    v |= __shfl_xor_sync(kFull, v, 4);
+                    const uint32_t wi = (base >> 5) + it * 4 + (lane >> 3);
+                    if ((lane & 7u) == 0 && wi * 32 < a.n) signw[wi] = v;
+                }
+            }
+            // zero padding of the tail code array and of the sign array
+            if (tc)
+                for (uint32_t i = tail + lane; i < (uint32_t)(pad16(2 * (uint64_t)tail) / 2); i += 32) tc[i] = 0;
             if (ND == 1 && signw) {
-                // 4 sign bits per lane -> one u32 per 8 lanes (32 consecutive elements)
-                uint32_t v = sgn << ((lane & 7u) * 4);
-                v |= __shfl_xor_sync(kFull, v, 1);
-                v |= __shfl_xor_sync(kFull, v, 2);
-                v |= __shfl_xor_sync(kFull, v, 4);
-                if ((lane & 7u) == 0) signw[(base >> 5) + it * 4 + (lane >> 3)] = v;
+                const uint32_t nsw = (uint32_t)cdiv(a.n, 32);
+                const uint32_t pw  = (uint32_t)(pad16(4 * (uint64_t)nsw) / 4);
+                for (uint32_t i = nsw + lane; i < pw; i += 32) signw[i] = 0;
+            }
+            // bitmap words of the partial block are zero (fz.cu:167), then the 16-byte pad
+            uint32_t*      A  = reinterpret_cast<uint32_t*>(a.out + a.off_a);
+            const uint32_t pa = (uint32_t)(pad16(4 * (uint64_t)a.nwords) / 4);
+            for (uint32_t i = a.nb * 8 + lane; i < pa; i += 32) A[i] = 0;
+        }
+
+        // ---- phase D: CTA total, then the tile's offset by decoupled look-back ----
+        ovf = __reduce_or_sync(kFull, ovf);
+        if (lane == 0) s_cnt[wid] = cnt, s_ovf[wid] = ovf;
+        __syncthreads();
+        if (wid == 0) {
+            const uint32_t c    = lane < kCompressWarps ? s_cnt[lane] : 0u;
+            const uint32_t o    = lane < kCompressWarps ? s_ovf[lane] : 0u;
+            const uint32_t tot  = __reduce_add_sync(kFull, c);
+            const uint32_t tov  = __reduce_or_sync(kFull, o);
+            uint32_t       excl = 0, povf = 0;
+            if (ct == 0) {
+                if (lane == 0) publish(a.state, 0, epoch, kFlagIncl, tov, tot);
+            } else {
+                if (lane == 0) publish(a.state, ct, epoch, kFlagAgg, tov, tot);
+                lookback(a.state, ct, epoch, a.status, excl, povf);
+                if (lane == 0) publish(a.state, ct, epoch, kFlagIncl, tov | povf, excl + tot);
+            }
+            if (lane == 0) {
+                s_excl = excl;
+                if (ct == nct - 1) {
+                    write_header(a, eb, tov | povf, excl + tot);
+                    if (a.boff) {
+                        // the total closes the offset table; zero its 16-byte pad
+                        a.boff[a.nb] = excl + tot;
+                        for (uint32_t i = a.nb + 1; i < (uint32_t)(pad16(4ull * (a.nb + 1)) / 4); ++i) a.boff[i] = 0;
+                    }
+                }
             }
         }
-        __syncwarp();
-        // ---- phase B: lane g transposes group g (words g*32 .. g*32+31) ----
-        uint32_t w[32];
-#pragma unroll
-        for (uint32_t tt = 0; tt < 8; ++tt) {
-            const uint4 v = *reinterpret_cast<const uint4*>(sm + swz(lane * 8 + tt));
-            w[4 * tt] = v.x, w[4 * tt + 1] = v.y, w[4 * tt + 2] = v.z, w[4 * tt + 3] = v.w;
+        __syncthreads();
+
+        // ---- phase E: block offset table, compacted 128-bit stores of the chunks ----
+        if (t < a.nb && a.boff && lane == 0) {
+            uint32_t pre = s_excl;
+            for (uint32_t w2 = 0; w2 < wid; ++w2) pre += s_cnt[w2];
+            a.boff[t] = pre;
         }
-        transpose32(w);
-        __syncwarp();
-        // shuffled image S[p*32 + g] = w[p] (bitshuffleAndBitflag's out, fz.cu:82)
+        if (t < a.nb && cnt) {
+            uint32_t pre = s_excl;
+            for (uint32_t w2 = 0; w2 < wid; ++w2) pre += s_cnt[w2];
+            uint4*         B  = reinterpret_cast<uint4*>(a.out + a.off_b);
+            const uint32_t lt = lanemask_lt();
 #pragma unroll
-        for (uint32_t p = 0; p < 32; ++p) sm[p * 32 + lane] = w[p];
-        __syncwarp();
-        // ---- phase C: chunk c = lane + 32 i; ballot i is bitmap word 8t+i ----
-#pragma unroll
-        for (uint32_t i = 0; i < 8; ++i) {
-            const uint4 v = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
-            bm[i] = __ballot_sync(kFull, (v.x | v.y | v.z | v.w) != 0);
-            cnt += __popc(bm[i]);
-        }
-        if (lane == 0) {
-            uint4* A = reinterpret_cast<uint4*>(a.out + a.off_a) + 2 * (size_t)t;
-            A[0]     = make_uint4(bm[0], bm[1], bm[2], bm[3]);
-            A[1]     = make_uint4(bm[4], bm[5], bm[6], bm[7]);
-        }
-    } else if (t == a.nb && a.n > base) {
-        // ---- tail block: n mod 2048 codes, never shuffled (fz.cu:173) ----
-        const uint32_t tail = a.n - base;
-        uint16_t*      tc   = (a.mode == 1) ? reinterpret_cast<uint16_t*>(a.out + a.off_c) : nullptr;
-        for (uint32_t it = 0; it * 128 < tail; ++it) {
-            const uint32_t e0 = base + it * 128 + lane * 4;
-            uint32_t       c[4], sgn = 0;
-            codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-                if (tc && e0 + j < a.n) tc[e0 + j - base] = (uint16_t)c[j];
-            if (ND == 1 && signw) {
-                uint32_t v = sgn << ((lane & 7u) * 4);
-                v |= __shfl_xor_sync(kFull, v, 1);
-                v |= __shfl_xor_sync(kFull, v, 2);
-                v |= __shfl_xor_sync(kFull, v, 4);
-                const uint32_t wi = (base >> 5) + it * 4 + (lane >> 3);
-                if ((lane & 7u) == 0 && wi * 32 < a.n) signw[wi] = v;
+            for (uint32_t i = 0; i < 8; ++i) {
+                if ((bm[i] >> lane) & 1u)
+                    B[pre + __popc(bm[i] & lt)] = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
+                pre += __popc(bm[i]);
             }
         }
-        // zero padding of the tail code array and of the sign array
-        if (tc)
-            for (uint32_t i = tail + lane; i < (uint32_t)(pad16(2 * (uint64_t)tail) / 2); i += 32) tc[i] = 0;
-        if (ND == 1 && signw) {
-            const uint32_t nsw = (uint32_t)cdiv(a.n, 32);
-            const uint32_t pw  = (uint32_t)(pad16(4 * (uint64_t)nsw) / 4);
-            for (uint32_t i = nsw + lane; i < pw; i += 32) signw[i] = 0;
-        }
-        // bitmap words of the partial block are zero (fz.cu:167), then the 16-byte pad
-        uint32_t*      A  = reinterpret_cast<uint32_t*>(a.out + a.off_a);
-        const uint32_t pa = (uint32_t)(pad16(4 * (uint64_t)a.nwords) / 4);
-        for (uint32_t i = a.nb * 8 + lane; i < pa; i += 32) A[i] = 0;
-    }
-
-    // ---- phase D: CTA total, then the CTA's offset by decoupled look-back ----
-    ovf = __reduce_or_sync(kFull, ovf);
-    if (lane == 0) s_cnt[wid] = cnt, s_ovf[wid] = ovf;
-    __syncthreads();
-    if (wid == 0) {
-        const uint32_t c   = lane < kCompressWarps ? s_cnt[lane] : 0u;
-        const uint32_t o   = lane < kCompressWarps ? s_ovf[lane] : 0u;
-        const uint32_t tot = __reduce_add_sync(kFull, c);
-        const uint32_t tov = __reduce_or_sync(kFull, o);
-        uint32_t       excl = 0, povf = 0;
-        if (ct == 0) {
-            if (lane == 0) publish(a.state, 0, a.epoch, kFlagIncl, tov, tot);
-        } else {
-            if (lane == 0) publish(a.state, ct, a.epoch, kFlagAgg, tov, tot);
-            lookback(a.state, ct, a.epoch, a.status, excl, povf);
-            if (lane == 0) publish(a.state, ct, a.epoch, kFlagIncl, tov | povf, excl + tot);
-        }
-        if (lane == 0) {
-            s_excl = excl;
-            if (ct == gridDim.x - 1) write_header(a, eb, tov | povf, excl + tot);
-        }
-    }
-    __syncthreads();
-    if (t >= a.nb || cnt == 0) return;
-
-    // ---- phase E: compacted 128-bit stores of the non-zero chunks ----
-    uint32_t pre = s_excl;
-    for (uint32_t w2 = 0; w2 < wid; ++w2) pre += s_cnt[w2];
-    uint4*         B  = reinterpret_cast<uint4*>(a.out + a.off_b);
-    const uint32_t lt = lanemask_lt();
-#pragma unroll
-    for (uint32_t i = 0; i < 8; ++i) {
-        if ((bm[i] >> lane) & 1u) B[pre + __popc(bm[i] & lt)] = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
-        pre += __popc(bm[i]);
+        __syncthreads();  // shared memory and cta_tile are reused by the next tile
     }
 }
 
 // One warp looks back from tile 1 at tile 0, which nothing publishes in this epoch: the
 // bounded wait must give up and raise kStatusTimeout (fz_selftest_wait_timeout).
-__global__ void k_wait_selftest(const uint64_t* state, uint32_t epoch, uint32_t* status)
+__global__ void k_wait_selftest(const uint64_t* state, const uint32_t* epoch, uint32_t* status)
 {
-    uint32_t excl = 0, ovf = 0;
-    lookback(state, 1, epoch, status, excl, ovf);
+    // the current device epoch has not been used by any launch yet
+    const uint32_t e    = __ldcg(epoch);
+    uint32_t       excl = 0, ovf = 0;
+    lookback(state, 1, e, status, excl, ovf);
 }
 
-cudaError_t launch_wait_selftest(const uint64_t* state, uint32_t epoch, uint32_t* status, cudaStream_t s)
+cudaError_t launch_wait_selftest(const uint64_t* state, const uint32_t* epoch, uint32_t* status, cudaStream_t s)
 {
     k_wait_selftest<<<1, 32, 0, s>>>(state, epoch, status);
     return cudaGetLastError();
 }
 
-cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* mm_next,
-                         uint32_t* status, cudaStream_t s)
+// Resident CTAs per SM of a kernel, and the SM count, queried once per process.
+template <typename K>
+static uint32_t resident_ctas(K kernel, int threads)
 {
-    const uint32_t ctas = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(cdiv(n / 4, 1024), 1), 4864);
-    k_range<<<ctas, 256, 0, s>>>(in, n, mm, mm_next, status);
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+    return (uint32_t)std::max(1, sms * std::max(per_sm, 1));
+}
+
+cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* status, cudaStream_t s)
+{
+    static const uint32_t wave = resident_ctas(k_range, 256);
+    const uint64_t        want = cdiv(n / 4, 256ull * kRangeUnroll);
+    const uint32_t        ctas = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, wave));
+    k_range<<<ctas, 256, 0, s>>>(in, n, mm, status);
     return cudaGetLastError();
 }
 
 cudaError_t launch_compress(const CompressArgs& a, cudaStream_t s)
 {
-    // one CTA per 8 shuffle blocks (the tail block included); a CTA is one scan tile
-    const uint32_t ctas = (uint32_t)cdiv(a.ntiles, kCompressWarps);
+    // persistent: min(tiles, one resident wave) CTAs; a tile is 8 shuffle blocks
+    static const uint32_t wave[3] = {resident_ctas(k_compress<1>, kCompressWarps * 32),
+                                     resident_ctas(k_compress<2>, kCompressWarps * 32),
+                                     resident_ctas(k_compress<3>, kCompressWarps * 32)};
+    const uint32_t nct  = (uint32_t)cdiv(a.ntiles, kCompressWarps);
+    const uint32_t ctas = std::min(nct, wave[a.ndim - 1]);
     switch (a.ndim) {
     case 1: k_compress<1><<<ctas, kCompressWarps * 32, 0, s>>>(a); break;
     case 2: k_compress<2><<<ctas, kCompressWarps * 32, 0, s>>>(a); break;
@@ -630,16 +675,17 @@ __global__ void __launch_bounds__(256) k_scan_encode(const uint8_t* __restrict__
                                                      uint32_t* presum, uint8_t* out,
                                                      uint64_t* state, uint32_t* ticket,
                                                      uint32_t* status, uint32_t* total,
-                                                     uint32_t epoch)
+                                                     uint32_t* epoch_word)
 {
-    __shared__ uint32_t cta_tile;
+    __shared__ uint32_t cta_tile, s_epoch;
     const uint32_t      lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
-        const uint32_t c = atomicAdd(ticket, 1u);
-        if (c == gridDim.x - 1) atomicExch(ticket, 0u);
-        cta_tile = c;
+        s_epoch = __ldcg(epoch_word);
+        __threadfence();
+        cta_tile = take_ticket(ticket, epoch_word, gridDim.x).tile;
     }
     __syncthreads();
+    const uint32_t epoch = s_epoch;
     const uint32_t t      = cta_tile * 8 + wid;
     const uint32_t ntiles = m / 256;  // m = 32 * ceil(n/256), a multiple of 32; tiles of 256
     const uint32_t ntl    = (m + 255) / 256;
@@ -687,7 +733,7 @@ __global__ void __launch_bounds__(256) k_scan_encode(const uint8_t* __restrict__
 cudaError_t launch_scan_encode(const uint8_t* shuffled, const uint32_t* byteflag,
                                uint32_t n_codes, uint32_t* presum, uint8_t* out,
                                uint64_t* state, uint32_t* ticket, uint32_t* status,
-                               uint32_t* total, uint32_t epoch, cudaStream_t s)
+                               uint32_t* total, uint32_t* epoch, cudaStream_t s)
 {
     const uint32_t m     = 32u * (uint32_t)cdiv(n_codes, 256);
     const uint32_t tiles = (uint32_t)cdiv(m, 256);

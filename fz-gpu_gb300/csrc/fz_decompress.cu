@@ -25,70 +25,119 @@ __device__ __forceinline__ uint32_t swz_d(uint32_t q)
     return ((g << 3) | (t ^ (g & 7u))) << 2;
 }
 
-__global__ void __launch_bounds__(kDecodeWarps * 32) k_decode(const DecodeArgs a)
+// ------------------------------------------------------------- offsets --
+// boff[b] = chunks of blocks 0..b-1 (the exclusive scan fz.cu:187-192 restricted to
+// block granularity), boff[nb] = the total, checked against the header's nnz.  One
+// thread per block (two 16-byte bitmap loads), CTAs of 256 chained by look-back.
+constexpr uint32_t kOffThreads = 256;
+
+__global__ void __launch_bounds__(kOffThreads) k_offsets(const uint8_t* __restrict__ st, uint64_t off_a,
+                                                        uint32_t nb, uint64_t nnz, uint32_t* boff,
+                                                        uint64_t* state, uint32_t* ticket,
+                                                        uint32_t* status, uint32_t* epoch_word)
 {
-    __shared__ __align__(16) uint32_t smem[kDecodeWarps][kBlockWords];
-    __shared__ uint32_t               s_cnt[kDecodeWarps];
-    __shared__ uint32_t               cta_tile, s_excl;
-    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-    uint32_t*      sm   = smem[wid];
+    __shared__ uint32_t s_w[kOffThreads / 32];
+    __shared__ uint32_t cta_tile, s_excl, s_epoch;
     if (threadIdx.x == 0) {
-        const uint32_t c = atomicAdd(a.ticket, 1u);
-        if (c == gridDim.x - 1) atomicExch(a.ticket, 0u);
-        cta_tile = c;
+        s_epoch = __ldcg(epoch_word);
+        __threadfence();
+        cta_tile = take_ticket(ticket, epoch_word, gridDim.x).tile;
     }
     __syncthreads();
-    const uint32_t ct = cta_tile;
-    const uint32_t t  = ct * kDecodeWarps + wid;
-
-    uint32_t bm[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cnt = 0;
-    if (t < a.nb) {
-        const uint4* A4 = reinterpret_cast<const uint4*>(a.st + a.off_a) + 2 * (size_t)t;
-        const uint4  b0 = __ldg(A4), b1 = __ldg(A4 + 1);
-        bm[0] = b0.x, bm[1] = b0.y, bm[2] = b0.z, bm[3] = b0.w;
-        bm[4] = b1.x, bm[5] = b1.y, bm[6] = b1.z, bm[7] = b1.w;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) cnt += __popc(bm[i]);
+    const uint32_t ct = cta_tile, lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const uint32_t epoch = s_epoch;
+    const uint32_t b  = ct * kOffThreads + threadIdx.x;
+    uint32_t       c  = 0;
+    if (b < nb) {
+        const uint4* A = reinterpret_cast<const uint4*>(st + off_a) + 2 * (size_t)b;
+        const uint4  u = __ldg(A), v = __ldg(A + 1);
+        c = __popc(u.x) + __popc(u.y) + __popc(u.z) + __popc(u.w) + __popc(v.x) + __popc(v.y) +
+            __popc(v.z) + __popc(v.w);
     }
-    // CTA total, then the CTA's first chunk by decoupled look-back
-    if (lane == 0) s_cnt[wid] = cnt;
+    uint32_t inc = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(kFull, inc, o);
+        if (lane >= (uint32_t)o) inc += u;
+    }
+    if (lane == 31) s_w[wid] = inc;
     __syncthreads();
     if (wid == 0) {
-        const uint32_t tot  = __reduce_add_sync(kFull, lane < kDecodeWarps ? s_cnt[lane] : 0u);
+        const uint32_t v = lane < kOffThreads / 32 ? s_w[lane] : 0u;
+        uint32_t       vi = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(kFull, vi, o);
+            if (lane >= (uint32_t)o) vi += u;
+        }
+        if (lane < kOffThreads / 32) s_w[lane] = vi - v;  // exclusive warp offsets
+        const uint32_t tot  = __shfl_sync(kFull, vi, 31);
         uint32_t       excl = 0, povf = 0;
         if (ct == 0) {
-            if (lane == 0) publish(a.state, 0, a.epoch, kFlagIncl, 0, tot);
+            if (lane == 0) publish(state, 0, epoch, kFlagIncl, 0, tot);
         } else {
-            if (lane == 0) publish(a.state, ct, a.epoch, kFlagAgg, 0, tot);
-            lookback(a.state, ct, a.epoch, a.status, excl, povf);
-            if (lane == 0) publish(a.state, ct, a.epoch, kFlagIncl, 0, excl + tot);
+            if (lane == 0) publish(state, ct, epoch, kFlagAgg, 0, tot);
+            lookback(state, ct, epoch, status, excl, povf);
+            if (lane == 0) publish(state, ct, epoch, kFlagIncl, 0, excl + tot);
         }
         if (lane == 0) {
             s_excl = excl;
-            if (ct == gridDim.x - 1 && excl + tot != a.nnz) atomicOr(a.status, kStatusCorrupt);
+            if (ct == gridDim.x - 1) {
+                boff[nb] = excl + tot;
+                if (excl + tot != nnz) atomicOr(status, kStatusCorrupt);
+            }
         }
     }
     __syncthreads();
+    if (b < nb) boff[b] = s_excl + s_w[wid] + inc - c;
+}
 
-    if (t < a.nb) {
-        uint32_t pre = s_excl;
-        for (uint32_t w2 = 0; w2 < wid; ++w2) pre += s_cnt[w2];
-        // gather: chunk c = lane + 32 i into the shuffled image S (words 4c..4c+3)
-        const uint4*   B   = reinterpret_cast<const uint4*>(a.st + a.off_b);
-        const uint32_t lt  = lanemask_lt();
-        bool           bad = false;
+cudaError_t launch_offsets(const uint8_t* st, uint64_t off_a, uint32_t nb, uint32_t nwords, uint64_t nnz,
+                           uint32_t* boff, uint64_t* state, uint32_t* ticket, uint32_t* status,
+                           uint32_t* epoch, cudaStream_t s)
+{
+    (void)nwords;
+    const uint32_t ctas = (uint32_t)std::max<uint64_t>(1, cdiv(nb, kOffThreads));
+    k_offsets<<<ctas, kOffThreads, 0, s>>>(st, off_a, nb, nnz, boff, state, ticket, status, epoch);
+    return cudaGetLastError();
+}
+
+// Gathers the shuffled image S of block t (words 4c..4c+3 of chunk c = lane + 32 i) into
+// shared memory; flagged chunks come from Section B in order, the others are zero.
+__device__ __forceinline__ void gather_block(const DecodeArgs& a, uint32_t t, uint32_t lane, uint32_t* sm)
+{
+    const uint4*   A4 = reinterpret_cast<const uint4*>(a.st + a.off_a) + 2 * (size_t)t;
+    const uint4    b0 = __ldg(A4), b1 = __ldg(A4 + 1);
+    const uint32_t bm[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+    const uint4*   B   = reinterpret_cast<const uint4*>(a.st + a.off_b);
+    const uint32_t lt  = lanemask_lt();
+    uint32_t       pre = __ldg(a.boff + t);
+    const uint32_t end = __ldg(a.boff + t + 1);
+    bool           bad = false;
 #pragma unroll
-        for (uint32_t i = 0; i < 8; ++i) {
-            uint4          v    = make_uint4(0, 0, 0, 0);
-            const uint32_t rank = pre + __popc(bm[i] & lt);
-            if ((bm[i] >> lane) & 1u) {
-                if (rank < a.nnz) v = __ldg(B + rank);
-                else bad = true;  // bitmap claims more chunks than the stream holds
-            }
-            *reinterpret_cast<uint4*>(sm + (lane + 32 * i) * 4) = v;
-            pre += __popc(bm[i]);
+    for (uint32_t i = 0; i < 8; ++i) {
+        uint4          v    = make_uint4(0, 0, 0, 0);
+        const uint32_t rank = pre + __popc(bm[i] & lt);
+        if ((bm[i] >> lane) & 1u) {
+            if (rank < a.nnz) v = __ldg(B + rank);
+            else bad = true;  // the bitmap claims more chunks than the stream holds
         }
-        if (bad) atomicOr(a.status, kStatusCorrupt);
+        *reinterpret_cast<uint4*>(sm + (lane + 32 * i) * 4) = v;
+        pre += __popc(bm[i]);
+    }
+    bad |= pre != end;  // bitmap and offset table disagree
+    if (bad) atomicOr(a.status, kStatusCorrupt);
+}
+
+// Two-pass path (3D and unaligned 2D): codes of every shuffle block into a scratch array.
+__global__ void __launch_bounds__(kDecodeWarps * 32) k_decode(const DecodeArgs a)
+{
+    __shared__ __align__(16) uint32_t smem[kDecodeWarps][kBlockWords];
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const uint32_t t    = blockIdx.x * kDecodeWarps + wid;
+    uint32_t*      sm   = smem[wid];
+    if (t < a.nb) {
+        gather_block(a, t, lane, sm);
         __syncwarp();
         // un-shuffle: W[g*32 + j] bit p = S[p*32 + g] bit j (the transpose is an involution)
         uint32_t w[32];
@@ -119,13 +168,222 @@ cudaError_t launch_decode(const DecodeArgs& a, cudaStream_t s)
     return cudaGetLastError();
 }
 
-// ------------------------------------------------------------- recon --
 __device__ __forceinline__ uint32_t sm_decode(uint32_t c)
 {
     const uint32_t mag = c & 0x7FFFu;
     return (c & 0x8000u) ? 0u - mag : mag;
 }
 
+// Decodes the 64 codes of group g (codes g*64 .. g*64+63) into 32 words w[j] =
+// code[2j] | code[2j+1] << 16.  Group gg of block b is word r4 = gg % 4 of the 32
+// chunks (p, k = gg / 4): its rank among the flagged chunks follows from the block's
+// bitmap and its offset boff[b].  Groups past the last full block read the sidecar.
+__device__ __forceinline__ void decode_group(const DecodeArgs& a, uint32_t g, uint32_t (&w)[32])
+{
+    const uint32_t b = g >> 5;
+    if (b < a.nb) {
+        const uint32_t gg = g & 31u, k = gg >> 2, r4 = gg & 3u;
+        const uint4*   A4 = reinterpret_cast<const uint4*>(a.st + a.off_a) + 2 * (size_t)b;
+        const uint4    b0 = __ldg(A4), b1 = __ldg(A4 + 1);
+        const uint32_t bm[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+        const uint32_t base  = __ldg(a.boff + b);
+        const uint32_t* W4   = reinterpret_cast<const uint32_t*>(a.st + a.off_b) + r4;
+        // chunk c = 8p + k sits in bitmap word p/4 at bit 8(p%4) + k
+        uint32_t lowm[4], bit[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            bit[q]  = 1u << (8 * q + k);
+            lowm[q] = bit[q] - 1u;
+        }
+        uint32_t pw  = base;
+        bool     bad = __ldg(a.boff + b + 1) - base !=
+                   (uint32_t)(__popc(b0.x) + __popc(b0.y) + __popc(b0.z) + __popc(b0.w) + __popc(b1.x) +
+                              __popc(b1.y) + __popc(b1.z) + __popc(b1.w));  // table vs bitmap
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int      p    = 4 * i + q;
+                const uint32_t rank = pw + __popc(bm[i] & lowm[q]);
+                uint32_t       v    = 0;
+                if (bm[i] & bit[q]) {
+                    if (rank < a.nnz) v = __ldg(W4 + 4 * (size_t)rank);
+                    else bad = true;
+                }
+                w[p] = v;
+            }
+            pw += __popc(bm[i]);
+        }
+        if (bad) atomicOr(a.status, kStatusCorrupt);
+        transpose32(w);  // w[p] = S[p*32 + gg]  ->  w[j] = W[gg*32 + j]
+    } else {
+        const uint16_t* tc  = a.mode == 1 ? reinterpret_cast<const uint16_t*>(a.st + a.off_c) : nullptr;
+        const uint32_t  e0  = g * 64;
+        const uint32_t  tb  = a.nb * kBlockCodes;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const uint32_t e  = e0 + 2 * j;
+            const uint32_t lo = (tc && e < a.n) ? tc[e - tb] : 0u;
+            const uint32_t hi = (tc && e + 1 < a.n) ? tc[e + 1 - tb] : 0u;
+            w[j] = lo | (hi << 16);
+        }
+    }
+}
+
+// ------------------------------------------------------ fused 2D decode --
+// A CTA owns the 16-row tile band blockIdx.y and the 960 columns blockIdx.x (60 tile
+// columns; rows a multiple of 4 elements).  Phase 1: thread (row rr, j) decodes group
+// glo(rr) + j of that row's span into a swizzled row buffer.  Phase 2: thread t owns
+// columns 4t..4t+3; prefix along x (serial + quad shuffles), running sum along y,
+// (float)p * ebx2, coalesced 16-byte stores.  Traffic: the chunks once (plus the at
+// most two groups a row shares with the next window) and the output once.
+constexpr uint32_t kW2 = 960;
+
+__global__ void __launch_bounds__(256) k_decompress2d(const DecodeArgs a)
+{
+    __shared__ __align__(16) uint32_t rows[16][512];  // 16 rows x 1024 codes
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    const uint32_t c0 = blockIdx.x * kW2, c1 = min(c0 + kW2, a.x);
+    const uint32_t r0 = blockIdx.y * 16;
+    {
+        const uint32_t rr = tid >> 4, j = tid & 15u, row = r0 + rr;
+        if (row < a.y) {
+            const uint32_t lin0 = row * a.x + c0, lin1 = row * a.x + c1;
+            const uint32_t g = (lin0 >> 6) + j;
+            if (g <= ((lin1 - 1) >> 6)) {
+                uint32_t w[32];
+                decode_group(a, g, w);
+                uint32_t* rb = rows[rr];
+#pragma unroll
+                for (uint32_t tt = 0; tt < 8; ++tt)
+                    *reinterpret_cast<uint4*>(rb + ((j * 8 + (tt ^ (j & 7u))) << 2)) =
+                        make_uint4(w[4 * tt], w[4 * tt + 1], w[4 * tt + 2], w[4 * tt + 3]);
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t col = c0 + 4 * tid;
+    const bool     live = col < c1;
+    const uint32_t q    = tid & 3u;
+    uint32_t       acc[4] = {0, 0, 0, 0};
+    for (uint32_t rr = 0; rr < 16; ++rr) {
+        const uint32_t row = r0 + rr;
+        if (row >= a.y) break;  // uniform across the CTA
+        uint32_t d[4] = {0, 0, 0, 0};
+        if (live) {
+            const uint32_t lin0 = row * a.x + c0;
+            const uint32_t i    = (lin0 & 63u) + 4 * tid;  // code index in the row buffer
+            const uint32_t G = i >> 6, c = (i >> 3) & 7u;
+            const uint2    v = *reinterpret_cast<const uint2*>(rows[rr] + ((G * 8 + (c ^ (G & 7u))) << 2) + ((i >> 2) & 1u) * 2);
+            d[0] = sm_decode(v.x & 0xFFFFu), d[1] = sm_decode(v.x >> 16);
+            d[2] = sm_decode(v.y & 0xFFFFu), d[3] = sm_decode(v.y >> 16);
+        }
+        d[1] += d[0], d[2] += d[1], d[3] += d[2];
+        uint32_t v = d[3];
+        uint32_t u = __shfl_up_sync(kFull, v, 1);
+        if (q >= 1) v += u;
+        u = __shfl_up_sync(kFull, v, 2);
+        if (q >= 2) v += u;
+        const uint32_t ex = v - d[3];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[j] += d[j] + ex;
+        if (live)
+            *reinterpret_cast<float4*>(a.out + (size_t)row * a.x + col) =
+                make_float4((float)(int32_t)acc[0] * a.ebx2, (float)(int32_t)acc[1] * a.ebx2,
+                            (float)(int32_t)acc[2] * a.ebx2, (float)(int32_t)acc[3] * a.ebx2);
+    }
+    (void)lane;
+}
+
+// ------------------------------------------------------ fused 1D decode --
+// One warp per shuffle block: lane g decodes its 64 codes (a quarter of one 256-element
+// x_lorenzo block), prefix-sums them serially, adds the quad's carry, and writes 64
+// floats through shared memory as coalesced 16-byte stores.  Codes at i%4 == 0 carry
+// their sign; the others take it from the sidecar sign bits (or are non-negative).
+constexpr int kDecode1dWarps = 4;
+
+__global__ void __launch_bounds__(kDecode1dWarps * 32) k_decompress1d(const DecodeArgs a)
+{
+    __shared__ __align__(16) uint32_t smem[kDecode1dWarps][2048];
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const uint32_t t    = blockIdx.x * kDecode1dWarps + wid;
+    const uint32_t ntiles = a.nb + (a.tail ? 1u : 0u);
+    if (t >= ntiles) return;  // warp-uniform
+    uint32_t* sm = smem[wid];
+    uint32_t  w[32];
+    if (t < a.nb) {
+        gather_block(a, t, lane, sm);
+        __syncwarp();
+#pragma unroll
+        for (uint32_t p = 0; p < 32; ++p) w[p] = sm[p * 32 + lane];
+        transpose32(w);
+        __syncwarp();
+    } else {
+        decode_group(a, t * 32 + lane, w);  // tail: sidecar codes
+    }
+    const uint32_t  e0 = t * kBlockCodes + lane * 64;
+    const uint32_t* sb = (a.mode == 1) ? reinterpret_cast<const uint32_t*>(a.st + a.off_sign) : nullptr;
+    uint32_t        s0 = 0, s1 = 0;
+    if (sb && e0 < a.n) {
+        s0 = __ldg(sb + (e0 >> 5));
+        s1 = (e0 + 32 < a.n) ? __ldg(sb + (e0 >> 5) + 1) : 0u;
+    }
+    uint32_t acc = 0;
+#pragma unroll
+    for (int j = 0; j < 64; ++j) {
+        const uint32_t c   = (j & 1) ? (w[j >> 1] >> 16) : (w[j >> 1] & 0xFFFFu);
+        const uint32_t sgn = ((j < 32 ? s0 >> j : s1 >> (j - 32)) & 1u);
+        const uint32_t d   = (j & 3) == 0 ? sm_decode(c) : (sgn ? 0u - c : c);
+        acc += (e0 + j < a.nl) ? d : 0u;
+        sm[(j ^ lane) + 64 * lane] = acc;  // lane-local run, swizzled so the 32 lanes hit 32 banks
+    }
+    // carry across the 4 lanes of each 256-element block
+    uint32_t v = acc, u = __shfl_up_sync(kFull, v, 1);
+    if (lane & 3u) v += u;
+    u = __shfl_up_sync(kFull, v, 2);
+    if ((lane & 3u) >= 2) v += u;
+    const uint32_t ex = v - acc;
+    __syncwarp();
+    // write: pass i covers elements i*128 .. i*128+127 of the block; lane owns 4
+    float* out = a.out + (size_t)t * kBlockCodes;
+    for (uint32_t i = 0; i < 16; ++i) {
+        const uint32_t el = i * 128 + lane * 4;   // element within the block
+        const uint32_t ow = el >> 6, j0 = el & 63u;  // owning lane, index in its run
+        const uint32_t exo = __shfl_sync(kFull, ex, ow);
+        float          f[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t j = j0 + k;
+            f[k] = (float)(int32_t)(sm[(j ^ ow) + 64 * ow] + exo) * a.ebx2;
+        }
+        const uint32_t e = t * kBlockCodes + el;
+        if (e + 3 < a.nl) {
+            *reinterpret_cast<float4*>(out + el) = make_float4(f[0], f[1], f[2], f[3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (e + k < a.nl) out[el + k] = f[k];
+        }
+    }
+}
+
+cudaError_t launch_decompress_fused(const DecodeArgs& a, cudaStream_t s)
+{
+    const int nd = (a.z == 1 && a.y == 1) ? 1 : (a.z == 1 ? 2 : 3);
+    if (nd == 2 && a.x % 4 == 0) {
+        dim3 grid((uint32_t)cdiv(a.x, kW2), (uint32_t)cdiv(a.y, 16));
+        k_decompress2d<<<grid, 256, 0, s>>>(a);
+        return cudaGetLastError();
+    }
+    if (nd == 1) {
+        const uint32_t ntiles = a.nb + (a.tail ? 1u : 0u);
+        k_decompress1d<<<(uint32_t)cdiv(ntiles, kDecode1dWarps), kDecode1dWarps * 32, 0, s>>>(a);
+        return cudaGetLastError();
+    }
+    return cudaErrorNotSupported;
+}
+
+// ------------------------------------------------------------- recon --
 // 2D: a CTA covers 16 rows x 512 columns; lane owns 4 consecutive columns, lanes 4k..4k+3
 // one 16-column tile row.  Row prefix: serial over 4 + quad shuffle scan; column prefix:
 // running sum over the 16 rows.
@@ -287,6 +545,12 @@ __global__ void __launch_bounds__(256) k_recon1d(const ReconArgs a)
 __global__ void k_zero_tail(float* out, uint32_t from, uint32_t n)
 {
     for (uint32_t i = from + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = 0.0f;
+}
+
+cudaError_t launch_zero_tail(float* out, uint32_t from, uint32_t n, cudaStream_t s)
+{
+    k_zero_tail<<<(uint32_t)std::min<uint64_t>(cdiv(n - from, 256), 1024), 256, 0, s>>>(out, from, n);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_reconstruct(const ReconArgs& a, cudaStream_t s)

@@ -120,17 +120,23 @@ __device__ __forceinline__ void transpose32(uint32_t (&a)[32])
 }
 
 // ------------------------------------------------------ scan tile state --
-// One u64 per tile: [epoch:28][flag:2][ovf:1][0:1][value:32].  flag 1 = aggregate
-// (this tile only), 2 = inclusive prefix.  A word from another epoch reads as "not
-// ready", so the array needs no clearing between calls.
+// One u64 per tile: [epoch:32][flag:2][ovf:1][value:29].  flag 1 = aggregate (this
+// tile only), 2 = inclusive prefix.  A word from another epoch reads as "not ready", so
+// the array needs no clearing between calls.  The epoch lives in device memory and is
+// advanced by each scanning kernel's last ticket fetch, so a kernel replayed from a
+// CUDA graph with frozen parameters still scans in a fresh epoch.  Values (chunk
+// counts) stay below 2^29 because a field holds at most 2^31 elements.
 constexpr uint64_t kFlagAgg  = 1;
 constexpr uint64_t kFlagIncl = 2;
 
 __device__ __forceinline__ uint64_t state_pack(uint32_t epoch, uint64_t flag, uint32_t ovf,
                                                uint32_t value)
 {
-    return ((uint64_t)epoch << 36) | (flag << 34) | ((uint64_t)(ovf & 1u) << 32) | value;
+    return ((uint64_t)epoch << 32) | (flag << 30) | ((uint64_t)(ovf & 1u) << 29) | (value & 0x1FFFFFFFu);
 }
+__device__ __forceinline__ uint32_t state_flag(uint64_t s) { return (uint32_t)(s >> 30) & 3u; }
+__device__ __forceinline__ uint32_t state_ovf(uint64_t s) { return (uint32_t)(s >> 29) & 1u; }
+__device__ __forceinline__ uint32_t state_value(uint64_t s) { return (uint32_t)s & 0x1FFFFFFFu; }
 // The value and its flag share one 64-bit word, so relaxed GPU-scope accesses suffice:
 // no other memory is published through it.
 __device__ __forceinline__ void st_state(uint64_t* p, uint64_t v)
@@ -170,7 +176,7 @@ __device__ __forceinline__ void lookback(const uint64_t* state, uint32_t t, uint
             for (int j = 0; j < 4; ++j) {
                 const int64_t pos = base - j;
                 s[j]     = pos >= 0 ? ld_state(state + pos) : state_pack(epoch, kFlagIncl, 0, 0);
-                ready[j] = (uint32_t)(s[j] >> 36) == epoch && ((s[j] >> 34) & 3u) != 0;
+                ready[j] = (uint32_t)(s[j] >> 32) == epoch && state_flag(s[j]) != 0;
                 all      = all && ready[j];
             }
             if (__all_sync(kFull, all)) break;
@@ -188,7 +194,7 @@ __device__ __forceinline__ void lookback(const uint64_t* state, uint32_t t, uint
         }
         uint32_t mine = 0;  // bit j: tile base-j holds an inclusive prefix
 #pragma unroll
-        for (int j = 0; j < 4; ++j) mine |= (((s[j] >> 34) & 3u) == kFlagIncl) ? (1u << j) : 0u;
+        for (int j = 0; j < 4; ++j) mine |= (state_flag(s[j]) == kFlagIncl) ? (1u << j) : 0u;
         const uint32_t any = __ballot_sync(kFull, mine != 0);
         // lanes before the first lane holding a prefix take all 4 tiles; that lane
         // takes its tiles up to its first prefix; later lanes take none
@@ -197,7 +203,7 @@ __device__ __forceinline__ void lookback(const uint64_t* state, uint32_t t, uint
         uint32_t  v = 0, o = 0;
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-            if (j <= jmax) v += (uint32_t)s[j], o |= (uint32_t)(s[j] >> 32) & 1u;
+            if (j <= jmax) v += state_value(s[j]), o |= state_ovf(s[j]);
         acc += __reduce_add_sync(kFull, v);
         acc_ovf |= __reduce_or_sync(kFull, o);
         if (any) break;
@@ -212,6 +218,27 @@ __device__ __forceinline__ void publish(uint64_t* state, uint32_t t, uint32_t ep
                                         uint64_t flag, uint32_t ovf, uint32_t value)
 {
     st_state(state + t, state_pack(epoch, flag, ovf, value));
+}
+
+// Ticket fetch of a scanning kernel: tiles are handed out in launch order (so every
+// predecessor of a tile has started and the look-back makes progress).  The last of the
+// `fetches` fetches of the launch resets the counter and advances the device epoch for
+// the next launch; every CTA reads the epoch before its first fetch.
+struct Ticket {
+    uint32_t tile;
+    bool     last;
+};
+__device__ __forceinline__ Ticket take_ticket(uint32_t* ticket, uint32_t* epoch_word, uint32_t fetches)
+{
+    Ticket         t;
+    const uint32_t c = atomicAdd(ticket, 1u);
+    t.tile           = c;
+    t.last           = (c == fetches - 1);
+    if (t.last) {
+        atomicExch(ticket, 0u);
+        atomicAdd(epoch_word, 1u);
+    }
+    return t;
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt()

@@ -18,7 +18,7 @@ struct Layout {
     uint32_t tail;     // n - 2048 nb
     uint32_t nwords;   // bitmap words ceil(n/256)
     uint32_t mode;
-    uint64_t off_a, off_c, off_b, off_sign;  // byte offsets in the stream
+    uint64_t off_a, off_c, off_b, off_sign, off_boff;  // byte offsets in the stream
     uint32_t sidecar_bytes;
 };
 Layout make_layout(uint64_t n, uint32_t x, uint32_t y, uint32_t z, uint32_t mode);
@@ -31,25 +31,26 @@ struct CompressArgs {
     FastDiv      dx, dxy;
     uint32_t     al_x, al_xy, al_xyx;  // 1 when the halo row offsets are multiples of 4
     uint32_t     nb, ntiles, nwords, mode, ndim, sidecar_bytes;
-    uint64_t     off_a, off_c, off_b, off_sign;
-    const uint32_t* mm;  // range-pass accumulators (relative eb), or null
+    uint64_t     off_a, off_c, off_b, off_sign, off_boff;
+    uint32_t*    mm;  // range-pass accumulators (relative eb), or null
     double       eb_rel; // relative error bound (with mm)
     EbInfo       ebh;    // constants computed on the host (absolute eb)
     uint64_t*    state;
     uint32_t*    ticket;
     uint32_t*    status;
-    uint32_t     epoch;
+    uint32_t*    epoch;  // device epoch word (advanced by the kernel's last ticket fetch)
+    uint32_t*    boff;   // block offset table in the stream's sidecar, or null
 };
 
 struct DecodeArgs {
-    const uint8_t* st;
-    uint16_t*      codes;  // scratch u16[n]
-    uint32_t       n, nb, tail, mode;
-    uint64_t       off_a, off_c, off_b, nnz;
-    uint64_t*      state;
-    uint32_t*      ticket;
-    uint32_t*      status;
-    uint32_t       epoch;
+    const uint8_t*  st;
+    uint16_t*       codes;    // scratch u16[n] (two-pass path)
+    const uint32_t* boff;     // chunk offset of each shuffle block (k_offsets)
+    float*          out;      // fused paths
+    uint32_t        n, nl, x, y, z, nb, tail, mode, nwords;
+    uint64_t        off_a, off_c, off_b, off_sign, off_boff, nnz;
+    float           ebx2;
+    uint32_t*       status;
 };
 
 struct ReconArgs {
@@ -62,13 +63,18 @@ struct ReconArgs {
 };
 
 // launchers (return the launch error)
-cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* mm_next,
-                         uint32_t* status, cudaStream_t s);
+cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* status, cudaStream_t s);
 cudaError_t launch_compress(const CompressArgs& a, cudaStream_t s);
+cudaError_t launch_offsets(const uint8_t* st, uint64_t off_a, uint32_t nb, uint32_t nwords, uint64_t nnz,
+                           uint32_t* boff, uint64_t* state, uint32_t* ticket, uint32_t* status,
+                           uint32_t* epoch, cudaStream_t s);
 cudaError_t launch_decode(const DecodeArgs& a, cudaStream_t s);
+// fused decode + inverse Lorenzo; returns cudaErrorNotSupported for shapes it does not cover
+cudaError_t launch_decompress_fused(const DecodeArgs& a, cudaStream_t s);
 cudaError_t launch_reconstruct(const ReconArgs& a, cudaStream_t s);
+cudaError_t launch_zero_tail(float* out, uint32_t from, uint32_t n, cudaStream_t s);
 
-cudaError_t launch_wait_selftest(const uint64_t* state, uint32_t epoch, uint32_t* status, cudaStream_t s);
+cudaError_t launch_wait_selftest(const uint64_t* state, const uint32_t* epoch, uint32_t* status, cudaStream_t s);
 
 // stage-level launchers
 cudaError_t launch_lorenzo_construct(const float* in, uint16_t* q, uint8_t* signum, uint32_t x,
@@ -78,7 +84,7 @@ cudaError_t launch_bitshuffle_flag(const uint32_t* in, uint32_t* out, uint32_t n
 cudaError_t launch_scan_encode(const uint8_t* shuffled, const uint32_t* byteflag,
                                uint32_t n_codes, uint32_t* presum, uint8_t* out,
                                uint64_t* state, uint32_t* ticket, uint32_t* status,
-                               uint32_t* total, uint32_t epoch, cudaStream_t s);
+                               uint32_t* total, uint32_t* epoch, cudaStream_t s);
 
 
 }  // namespace fz

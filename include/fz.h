@@ -148,8 +148,9 @@ fz_status fz_workspace_status(fz_workspace* ws, fz_stream_t stream);
    pair of CUDA events on the call's stream.  capacity 0 disables it. */
 fz_status fz_workspace_enable_timing(fz_workspace* ws, uint32_t capacity);
 /* Number of recorded launches of one kernel kind (0 range pass, 1 fused compress,
-   2 decode, 3 inverse Lorenzo) and their summed duration; syncs on the last recorded
-   event and frees those records. */
+   2 block offsets, 3 decode -- fused with the inverse Lorenzo for 1D and for 2D rows
+   of a multiple of 4 elements --, 4 separate inverse Lorenzo) and their summed
+   duration; syncs on the last recorded event and frees those records. */
 fz_status fz_workspace_kernel_time(fz_workspace* ws, int kind, uint32_t* launches,
                                    double* total_ms);
 
@@ -219,6 +220,41 @@ fz_status fz_bitshuffle_flag(const uint32_t* d_in, uint32_t* d_out, uint64_t n_c
 fz_status fz_scan_encode(fz_workspace* ws, const uint8_t* d_shuffled,
                          const uint32_t* d_byteflag, uint64_t n_codes, uint32_t* d_presum,
                          uint8_t* d_out, uint64_t* nnz, fz_stream_t stream);
+
+/* ------------------------------------------------------------- batching -- */
+/* One field of a batch.  Compression reads src (float[n], dims, eb) and writes the
+   stream to dst (dst_capacity bytes, at least fz_max_compressed_bytes); decompression
+   reads the stream src (src_bytes, with its header copied to `header`) and writes
+   dst (dst_capacity elements). */
+typedef struct fz_field {
+    const void* src;
+    void*       dst;
+    uint64_t    n;
+    fz_dims     dims;
+    double      eb;
+    uint64_t    dst_capacity;
+    uint64_t    src_bytes;
+    fz_header   header;
+} fz_field;
+
+typedef enum fz_direction { FZ_COMPRESS = 0, FZ_DECOMPRESS = 1 } fz_direction;
+
+/* Enqueues the whole batch on `stream` in one call (fields in order, one workspace:
+   its capacity must cover the largest field).  No counterpart in the reference,
+   which handles one file per process (fz.cu:226-238). */
+fz_status fz_compress_batch(fz_workspace* ws, const fz_field* fields, uint32_t count,
+                            fz_eb_mode eb_mode, fz_mode mode, fz_stream_t stream);
+fz_status fz_decompress_batch(fz_workspace* ws, const fz_field* fields, uint32_t count,
+                              fz_stream_t stream);
+
+/* A batch recorded once into a CUDA graph and replayed with fz_batch_launch; the
+   buffers of `fields` must stay valid while the batch exists.  The scan state's epoch
+   is kept in device memory, so replays with frozen kernel parameters stay correct. */
+typedef struct fz_batch fz_batch;
+fz_status fz_batch_create(fz_workspace* ws, const fz_field* fields, uint32_t count,
+                          fz_direction dir, fz_eb_mode eb_mode, fz_mode mode, fz_batch** out);
+fz_status fz_batch_launch(fz_batch* batch, fz_stream_t stream);
+fz_status fz_batch_destroy(fz_batch* batch);
 
 #ifdef __cplusplus
 }

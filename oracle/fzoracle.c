@@ -264,8 +264,9 @@ void fzo_layout(uint64_t n, int ndim, int mode, uint64_t* off_a, uint64_t* off_c
     uint64_t c  = a + pad16(4 * nw);
     uint64_t sc = 0;
     if (mode == 1) {
-        sc += pad16(2 * (n % BLOCK_CODES));        /* raw tail codes */
+        sc += pad16(2 * (n % BLOCK_CODES));          /* raw tail codes */
         if (ndim == 1) sc += pad16(4 * cdiv(n, 32)); /* 1D sign bits */
+        sc += pad16(4 * (n / BLOCK_CODES + 1));      /* chunk offset of each shuffle block */
     }
     *off_a         = a;
     *off_c         = c;
@@ -316,10 +317,19 @@ uint64_t fzo_compress(const float* data, uint64_t n, uint32_t x, uint32_t y, uin
         uint64_t nb   = n / BLOCK_CODES;
         uint64_t tail = n - nb * BLOCK_CODES;
         memcpy(out + off_c, codes + nb * BLOCK_CODES, tail * 2);
+        uint64_t q = off_c + pad16(2 * tail);
         if (nd == 1) {
-            uint8_t* sb = out + off_c + pad16(2 * tail);
+            uint8_t* sb = out + q;
             for (uint64_t i = 0; i < n; i++)
                 if (sg[i]) sb[i >> 3] |= (uint8_t)(1u << (i & 7));
+            q += pad16(4 * cdiv(n, 32));
+        }
+        /* boff[b] = chunks of blocks 0..b-1, boff[nb] = nnz */
+        uint32_t acc = 0;
+        for (uint64_t b = 0; b <= nb; b++) {
+            put32(out + q + 4 * b, acc);
+            if (b < nb)
+                for (int k = 0; k < 8; k++) acc += (uint32_t)__builtin_popcount(B[b * 8 + k]);
         }
     }
     /* header (include/fz.h, struct fz_header) */
@@ -482,6 +492,17 @@ int fzo_decompress(const uint8_t* st, uint64_t bytes, float* out, uint64_t n_cap
             free(boff);
             return -5;
         }
+    if (mode == 1) {
+        /* the sidecar's block offsets must agree with the bitmap */
+        uint64_t tail = n - nb * BLOCK_CODES;
+        uint64_t q    = off_c + pad16(2 * tail) + (nd == 1 ? pad16(4 * cdiv(n, 32)) : 0);
+        for (uint64_t b = 0; b <= nb; b++)
+            if (get32(st + q + 4 * b) != (b < nb ? boff[b] : nnz)) {
+                free(codes);
+                free(boff);
+                return -6;
+            }
+    }
 #pragma omp parallel for schedule(static)
     for (uint64_t b = 0; b < nb; b++) {
         uint32_t s[BLOCK_WORDS];

@@ -179,7 +179,9 @@ def test_stream_header_and_sections(oracle, synth):
     assert h["range"] == np.float32(mx - mn)
     assert h["eb_abs"] == 1e-3 * float(np.float32(mx - mn))
     a, c, b, sc = oracle.layout(data.size, 2, 1)
-    assert sc == h["sidecar_bytes"] == 16 * ((2 * (data.size % 2048) + 15) // 16)
+    pad = lambda v: 16 * ((v + 15) // 16)
+    nb = data.size // 2048
+    assert sc == h["sidecar_bytes"] == pad(2 * (data.size % 2048)) + pad(4 * (nb + 1))
     codes, _, _ = oracle.lorenzo_construct(data, (200, 50, 1), h["ebx2_r"])
     S, F, B = oracle.bitshuffle_flag(codes)
     assert np.array_equal(st[a: a + 4 * B.size].view(np.uint32), B)
@@ -187,6 +189,11 @@ def test_stream_header_and_sections(oracle, synth):
     assert nnz == h["nnz"] and np.array_equal(st[b:], out)
     tail = data.size % 2048
     assert np.array_equal(st[c: c + 2 * tail].view(np.uint16), codes[data.size - tail:])
+    # chunk offset of every shuffle block, then the total
+    q = c + pad(2 * tail)
+    boff = st[q: q + 4 * (nb + 1)].view(np.uint32)
+    counts = np.array([sum(bin(int(w)).count("1") for w in B[8 * i: 8 * i + 8]) for i in range(nb)])
+    assert np.array_equal(boff, np.concatenate([[0], np.cumsum(counts)]).astype(np.uint32))
 
 
 def test_nonfinite_relative_eb_rejected(oracle):
