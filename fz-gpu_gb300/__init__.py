@@ -87,6 +87,7 @@ SIGNATURES = {
     "fz_workspace_kernel_time": (_I, [_P, _I, C.POINTER(C.c_uint32), C.POINTER(C.c_double)]),
     "fz_compress": (_I, [_P, _P, _U64, Dims, _D, _I, _I, _P, _U64, _PU64, _P]),
     "fz_decompress": (_I, [_P, _P, _U64, C.POINTER(Header), _P, _U64, _P]),
+    "fz_compress_noalloc": (_I, [_P, _U64, Dims, _D, _I, _I, _P, _U64, _PU64, _P]),
     "fz_compress_host": (_I, [_P, _P, _U64, Dims, _D, _I, _I, _P, _U64, _PU64, _P]),
     "fz_decompress_host": (_I, [_P, _P, _U64, _P, _U64, _P]),
     "fz_lorenzo_construct": (_I, [_P, _P, _P, Dims, _D, _P]),
