@@ -338,17 +338,22 @@ __device__ __forceinline__ uint32_t swz(uint32_t q)
 // Persistent: one resident wave of CTAs; each CTA repeatedly takes the next scan tile
 // (8 shuffle blocks, one per warp) from the ticket counter.  Tickets are handed out in
 // order, so every predecessor of a tile has been taken by a running CTA and the
-// look-back always makes progress.  The last of the nctiles + gridDim.x fetches resets
-// the counter for the next call.
+// look-back always makes progress.  The last of the nct + gridDim.x fetches resets the
+// counter, the range accumulators and advances the epoch.
+//
+// Software pipeline over a CTA's tiles, shared memory double-buffered: iteration k
+// computes tile k (codes, transposes, flags, aggregate published), then resolves tile
+// k-1 (look-back, offsets, compacted stores).  By then tile k-1's predecessors have long
+// published their inclusive prefixes, so its look-back is about one round trip instead
+// of a walk past every tile in flight.
 template <int ND>
 __global__ void __launch_bounds__(kCompressWarps * 32) k_compress(const CompressArgs a)
 {
-    __shared__ __align__(16) uint32_t smem[kCompressWarps][kBlockWords];
-    __shared__ uint32_t               s_cnt[kCompressWarps], s_ovf[kCompressWarps];
-    __shared__ uint32_t               cta_tile, s_excl, s_epoch;
-    __shared__ EbInfo                 s_eb;
+    extern __shared__ __align__(16) uint32_t dsm[];  // [2][kCompressWarps][kBlockWords]
+    __shared__ uint32_t s_cnt[2][kCompressWarps], s_ovf[2][kCompressWarps], s_tile[2], s_tot[2];
+    __shared__ uint32_t s_excl, s_epoch;
+    __shared__ EbInfo   s_eb;
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-    uint32_t*      sm   = smem[wid];
     const uint32_t nct  = (uint32_t)cdiv(a.ntiles, kCompressWarps);
 
     if (threadIdx.x == 0) {
@@ -360,153 +365,169 @@ __global__ void __launch_bounds__(kCompressWarps * 32) k_compress(const Compress
     g.nl = a.nl, g.x = a.x, g.y = a.y, g.xy = a.xy, g.lim = a.n;
     g.dx = a.dx, g.dxy = a.dxy, g.al_x = a.al_x, g.al_xy = a.al_xy, g.al_xyx = a.al_xyx;
     uint32_t* signw = (ND == 1 && a.mode == 1) ? reinterpret_cast<uint32_t*>(a.out + a.off_sign) : nullptr;
+    uint32_t  bm_prev[8];  // bitmap words of this warp's block of the previous tile
 
-    while (true) {
+    for (uint32_t k = 0;; ++k) {
+        const uint32_t buf = k & 1u;
+        uint32_t*      sm  = dsm + (buf * kCompressWarps + wid) * kBlockWords;
         if (threadIdx.x == 0) {
             const Ticket tk = take_ticket(a.ticket, a.epoch, nct + gridDim.x);
             if (tk.last && a.mm) a.mm[0] = 0xFFFFFFFFu, a.mm[1] = 0u;  // empty range for the next call
-            cta_tile = tk.tile;
+            s_tile[buf] = tk.tile;
         }
         __syncthreads();
-        const uint32_t ct    = cta_tile;
+        const uint32_t ct    = s_tile[buf];
+        const bool     have  = ct < nct;  // uniform
+        const EbInfo   eb    = s_eb;
         const uint32_t epoch = s_epoch;
-        if (ct >= nct) break;  // uniform
-        const EbInfo   eb   = s_eb;
-        const float    r    = eb.ebx2_r;
-        const uint32_t t    = ct * kCompressWarps + wid;  // this warp's shuffle block
-        const uint32_t base = t * kBlockCodes;
-        uint32_t       ovf  = 0, cnt = 0;
         uint32_t       bm[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
-        if (t < a.nb) {
-            // ---- phase A: codes of the block into shared memory (swizzled) ----
+        if (have) {
+            const float    r    = eb.ebx2_r;
+            const uint32_t t    = ct * kCompressWarps + wid;  // this warp's shuffle block
+            const uint32_t base = t * kBlockCodes;
+            uint32_t       ovf  = 0, cnt = 0;
+            if (t < a.nb) {
+                // ---- phase A: codes of the block into shared memory (swizzled) ----
 #pragma unroll 2
-            for (uint32_t it = 0; it < 16; ++it) {
-                const uint32_t e0 = base + it * 128 + lane * 4;
-                uint32_t       c[4], sgn = 0;
-                codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
-                const uint32_t q = it * 16 + (lane >> 1);
-                *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
-                    make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
-                if (ND == 1 && signw) {
-                    // 4 sign bits per lane -> one u32 per 8 lanes (32 consecutive elements)
-                    uint32_t v = sgn << ((lane & 7u) * 4);
-                    v |= __shfl_xor_sync(kFull, v, 1);
-                    v |= __shfl_xor_sync(kFull, v, 2);
-                    v |= __shfl_xor_sync(kFull, v, 4);
-                    if ((lane & 7u) == 0) signw[(base >> 5) + it * 4 + (lane >> 3)] = v;
+                for (uint32_t it = 0; it < 16; ++it) {
+                    const uint32_t e0 = base + it * 128 + lane * 4;
+                    uint32_t       c[4], sgn = 0;
+                    codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
+                    const uint32_t q = it * 16 + (lane >> 1);
+                    *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
+                        make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+                    if (ND == 1 && signw) {
+                        // 4 sign bits per lane -> one u32 per 8 lanes (32 consecutive elements)
+                        uint32_t v = sgn << ((lane & 7u) * 4);
+                        v |= __shfl_xor_sync(kFull, v, 1);
+                        v |= __shfl_xor_sync(kFull, v, 2);
+                        v |= __shfl_xor_sync(kFull, v, 4);
+                        if ((lane & 7u) == 0) signw[(base >> 5) + it * 4 + (lane >> 3)] = v;
+                    }
                 }
-            }
-            __syncwarp();
-            // ---- phase B: lane g transposes group g (words g*32 .. g*32+31) ----
-            uint32_t w[32];
+                __syncwarp();
+                // ---- phase B: lane g transposes group g (words g*32 .. g*32+31) ----
+                uint32_t w[32];
 #pragma unroll
-            for (uint32_t tt = 0; tt < 8; ++tt) {
-                const uint4 v = *reinterpret_cast<const uint4*>(sm + swz(lane * 8 + tt));
-                w[4 * tt] = v.x, w[4 * tt + 1] = v.y, w[4 * tt + 2] = v.z, w[4 * tt + 3] = v.w;
-            }
-            transpose32(w);
-            __syncwarp();
-            // shuffled image S[p*32 + g] = w[p] (bitshuffleAndBitflag's out, fz.cu:82)
-#pragma unroll
-            for (uint32_t p = 0; p < 32; ++p) sm[p * 32 + lane] = w[p];
-            __syncwarp();
-            // ---- phase C: chunk c = lane + 32 i; ballot i is bitmap word 8t+i ----
-#pragma unroll
-            for (uint32_t i = 0; i < 8; ++i) {
-                const uint4 v = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
-                bm[i] = __ballot_sync(kFull, (v.x | v.y | v.z | v.w) != 0);
-                cnt += __popc(bm[i]);
-            }
-            if (lane == 0) {
-                uint4* A = reinterpret_cast<uint4*>(a.out + a.off_a) + 2 * (size_t)t;
-                A[0]     = make_uint4(bm[0], bm[1], bm[2], bm[3]);
-                A[1]     = make_uint4(bm[4], bm[5], bm[6], bm[7]);
-            }
-        } else if (t == a.nb && a.n > base) {
-            // ---- tail block: n mod 2048 codes, never shuffled (fz.cu:173) ----
-            const uint32_t tail = a.n - base;
-            uint16_t*      tc   = (a.mode == 1) ? reinterpret_cast<uint16_t*>(a.out + a.off_c) : nullptr;
-            for (uint32_t it = 0; it * 128 < tail; ++it) {
-                const uint32_t e0 = base + it * 128 + lane * 4;
-                uint32_t       c[4], sgn = 0;
-                codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    if (tc && e0 + j < a.n) tc[e0 + j - base] = (uint16_t)c[j];
-                if (ND == 1 && signw) {
-                    uint32_t v = sgn << ((lane & 7u) * 4);
-                    v |= __shfl_xor_sync(kFull, v, 1);
-                    v |= __shfl_xor_sync(kFull, v, 2);
-                    v |= __shfl_xor_sync(kFull, v, 4);
-                    const uint32_t wi = (base >> 5) + it * 4 + (lane >> 3);
-                    if ((lane & 7u) == 0 && wi * 32 < a.n) signw[wi] = v;
+                for (uint32_t tt = 0; tt < 8; ++tt) {
+                    const uint4 v = *reinterpret_cast<const uint4*>(sm + swz(lane * 8 + tt));
+                    w[4 * tt] = v.x, w[4 * tt + 1] = v.y, w[4 * tt + 2] = v.z, w[4 * tt + 3] = v.w;
                 }
+                transpose32(w);
+                __syncwarp();
+                // shuffled image S[p*32 + g] = w[p] (bitshuffleAndBitflag's out, fz.cu:82)
+#pragma unroll
+                for (uint32_t p = 0; p < 32; ++p) sm[p * 32 + lane] = w[p];
+                __syncwarp();
+                // ---- phase C: chunk c = lane + 32 i; ballot i is bitmap word 8t+i ----
+#pragma unroll
+                for (uint32_t i = 0; i < 8; ++i) {
+                    const uint4 v = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
+                    bm[i] = __ballot_sync(kFull, (v.x | v.y | v.z | v.w) != 0);
+                    cnt += __popc(bm[i]);
+                }
+                if (lane == 0) {
+                    uint4* A = reinterpret_cast<uint4*>(a.out + a.off_a) + 2 * (size_t)t;
+                    A[0]     = make_uint4(bm[0], bm[1], bm[2], bm[3]);
+                    A[1]     = make_uint4(bm[4], bm[5], bm[6], bm[7]);
+                }
+            } else if (t == a.nb && a.n > base) {
+                // ---- tail block: n mod 2048 codes, never shuffled (fz.cu:173) ----
+                const uint32_t tail = a.n - base;
+                uint16_t*      tc   = (a.mode == 1) ? reinterpret_cast<uint16_t*>(a.out + a.off_c) : nullptr;
+                for (uint32_t it = 0; it * 128 < tail; ++it) {
+                    const uint32_t e0 = base + it * 128 + lane * 4;
+                    uint32_t       c[4], sgn = 0;
+                    codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (tc && e0 + j < a.n) tc[e0 + j - base] = (uint16_t)c[j];
+                    if (ND == 1 && signw) {
+                        uint32_t v = sgn << ((lane & 7u) * 4);
+                        v |= __shfl_xor_sync(kFull, v, 1);
+                        v |= __shfl_xor_sync(kFull, v, 2);
+                        v |= __shfl_xor_sync(kFull, v, 4);
+                        const uint32_t wi = (base >> 5) + it * 4 + (lane >> 3);
+                        if ((lane & 7u) == 0 && wi * 32 < a.n) signw[wi] = v;
+                    }
+                }
+                // zero padding of the tail code array and of the sign array
+                if (tc)
+                    for (uint32_t i = tail + lane; i < (uint32_t)(pad16(2 * (uint64_t)tail) / 2); i += 32) tc[i] = 0;
+                if (ND == 1 && signw) {
+                    const uint32_t nsw = (uint32_t)cdiv(a.n, 32);
+                    const uint32_t pw  = (uint32_t)(pad16(4 * (uint64_t)nsw) / 4);
+                    for (uint32_t i = nsw + lane; i < pw; i += 32) signw[i] = 0;
+                }
+                // bitmap words of the partial block are zero (fz.cu:167), then the 16-byte pad
+                uint32_t*      A  = reinterpret_cast<uint32_t*>(a.out + a.off_a);
+                const uint32_t pa = (uint32_t)(pad16(4 * (uint64_t)a.nwords) / 4);
+                for (uint32_t i = a.nb * 8 + lane; i < pa; i += 32) A[i] = 0;
             }
-            // zero padding of the tail code array and of the sign array
-            if (tc)
-                for (uint32_t i = tail + lane; i < (uint32_t)(pad16(2 * (uint64_t)tail) / 2); i += 32) tc[i] = 0;
-            if (ND == 1 && signw) {
-                const uint32_t nsw = (uint32_t)cdiv(a.n, 32);
-                const uint32_t pw  = (uint32_t)(pad16(4 * (uint64_t)nsw) / 4);
-                for (uint32_t i = nsw + lane; i < pw; i += 32) signw[i] = 0;
-            }
-            // bitmap words of the partial block are zero (fz.cu:167), then the 16-byte pad
-            uint32_t*      A  = reinterpret_cast<uint32_t*>(a.out + a.off_a);
-            const uint32_t pa = (uint32_t)(pad16(4 * (uint64_t)a.nwords) / 4);
-            for (uint32_t i = a.nb * 8 + lane; i < pa; i += 32) A[i] = 0;
+            ovf = __reduce_or_sync(kFull, ovf);
+            if (lane == 0) s_cnt[buf][wid] = cnt, s_ovf[buf][wid] = ovf;
         }
-
-        // ---- phase D: CTA total, then the tile's offset by decoupled look-back ----
-        ovf = __reduce_or_sync(kFull, ovf);
-        if (lane == 0) s_cnt[wid] = cnt, s_ovf[wid] = ovf;
         __syncthreads();
+        // ---- tile k: CTA aggregate published; tile k-1: look-back and offset ----
         if (wid == 0) {
-            const uint32_t c    = lane < kCompressWarps ? s_cnt[lane] : 0u;
-            const uint32_t o    = lane < kCompressWarps ? s_ovf[lane] : 0u;
-            const uint32_t tot  = __reduce_add_sync(kFull, c);
-            const uint32_t tov  = __reduce_or_sync(kFull, o);
-            uint32_t       excl = 0, povf = 0;
-            if (ct == 0) {
-                if (lane == 0) publish(a.state, 0, epoch, kFlagIncl, tov, tot);
-            } else {
-                if (lane == 0) publish(a.state, ct, epoch, kFlagAgg, tov, tot);
-                lookback(a.state, ct, epoch, a.status, excl, povf);
-                if (lane == 0) publish(a.state, ct, epoch, kFlagIncl, tov | povf, excl + tot);
+            if (have) {
+                const uint32_t tot = __reduce_add_sync(kFull, lane < kCompressWarps ? s_cnt[buf][lane] : 0u);
+                const uint32_t tov = __reduce_or_sync(kFull, lane < kCompressWarps ? s_ovf[buf][lane] : 0u);
+                if (lane == 0) {
+                    s_tot[buf] = tot;
+                    if (ct == 0) publish(a.state, 0, epoch, kFlagIncl, tov, tot);
+                    else publish(a.state, ct, epoch, kFlagAgg, tov, tot);
+                }
             }
-            if (lane == 0) {
-                s_excl = excl;
-                if (ct == nct - 1) {
-                    write_header(a, eb, tov | povf, excl + tot);
-                    if (a.boff) {
-                        // the total closes the offset table; zero its 16-byte pad
-                        a.boff[a.nb] = excl + tot;
-                        for (uint32_t i = a.nb + 1; i < (uint32_t)(pad16(4ull * (a.nb + 1)) / 4); ++i) a.boff[i] = 0;
+            if (k > 0) {
+                const uint32_t pb  = buf ^ 1u;
+                const uint32_t pct = s_tile[pb];
+                const uint32_t tot = s_tot[pb];
+                const uint32_t tov = __reduce_or_sync(kFull, lane < kCompressWarps ? s_ovf[pb][lane] : 0u);
+                uint32_t       excl = 0, povf = 0;
+                if (pct != 0) {
+                    lookback(a.state, pct, epoch, a.status, excl, povf);
+                    if (lane == 0) publish(a.state, pct, epoch, kFlagIncl, tov | povf, excl + tot);
+                }
+                if (lane == 0) {
+                    s_excl = excl;
+                    if (pct == nct - 1) {
+                        write_header(a, eb, tov | povf, excl + tot);
+                        if (a.boff) {
+                            // the total closes the offset table; zero its 16-byte pad
+                            a.boff[a.nb] = excl + tot;
+                            for (uint32_t i = a.nb + 1; i < (uint32_t)(pad16(4ull * (a.nb + 1)) / 4); ++i) a.boff[i] = 0;
+                        }
                     }
                 }
             }
         }
         __syncthreads();
-
-        // ---- phase E: block offset table, compacted 128-bit stores of the chunks ----
-        if (t < a.nb && a.boff && lane == 0) {
-            uint32_t pre = s_excl;
-            for (uint32_t w2 = 0; w2 < wid; ++w2) pre += s_cnt[w2];
-            a.boff[t] = pre;
-        }
-        if (t < a.nb && cnt) {
-            uint32_t pre = s_excl;
-            for (uint32_t w2 = 0; w2 < wid; ++w2) pre += s_cnt[w2];
-            uint4*         B  = reinterpret_cast<uint4*>(a.out + a.off_b);
-            const uint32_t lt = lanemask_lt();
+        // ---- tile k-1: block offset table and compacted 128-bit stores ----
+        if (k > 0) {
+            const uint32_t pb = buf ^ 1u;
+            const uint32_t t  = s_tile[pb] * kCompressWarps + wid;
+            if (t < a.nb) {
+                uint32_t pre = s_excl;
+                for (uint32_t w2 = 0; w2 < wid; ++w2) pre += s_cnt[pb][w2];
+                if (a.boff && lane == 0) a.boff[t] = pre;
+                const uint32_t* smp = dsm + (pb * kCompressWarps + wid) * kBlockWords;
+                uint4*          B   = reinterpret_cast<uint4*>(a.out + a.off_b);
+                const uint32_t  lt  = lanemask_lt();
 #pragma unroll
-            for (uint32_t i = 0; i < 8; ++i) {
-                if ((bm[i] >> lane) & 1u)
-                    B[pre + __popc(bm[i] & lt)] = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
-                pre += __popc(bm[i]);
+                for (uint32_t i = 0; i < 8; ++i) {
+                    if ((bm_prev[i] >> lane) & 1u)
+                        B[pre + __popc(bm_prev[i] & lt)] = *reinterpret_cast<const uint4*>(smp + (lane + 32 * i) * 4);
+                    pre += __popc(bm_prev[i]);
+                }
             }
         }
-        __syncthreads();  // shared memory and cta_tile are reused by the next tile
+        if (!have) break;  // uniform; tile k-1 (if any) has been resolved above
+#pragma unroll
+        for (int i = 0; i < 8; ++i) bm_prev[i] = bm[i];
+        // the next iteration rewrites slot and buffer k+1 & 1, which phase E just read
+        __syncthreads();
     }
 }
 
@@ -528,12 +549,13 @@ cudaError_t launch_wait_selftest(const uint64_t* state, const uint32_t* epoch, u
 
 // Resident CTAs per SM of a kernel, and the SM count, queried once per process.
 template <typename K>
-static uint32_t resident_ctas(K kernel, int threads)
+static uint32_t resident_ctas(K kernel, int threads, int dyn_smem = 0)
 {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+    if (dyn_smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, dyn_smem);
     return (uint32_t)std::max(1, sms * std::max(per_sm, 1));
 }
 
@@ -549,15 +571,16 @@ cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* st
 cudaError_t launch_compress(const CompressArgs& a, cudaStream_t s)
 {
     // persistent: min(tiles, one resident wave) CTAs; a tile is 8 shuffle blocks
-    static const uint32_t wave[3] = {resident_ctas(k_compress<1>, kCompressWarps * 32),
-                                     resident_ctas(k_compress<2>, kCompressWarps * 32),
-                                     resident_ctas(k_compress<3>, kCompressWarps * 32)};
+    constexpr int         kSmem   = 2 * kCompressWarps * kBlockWords * 4;  // two tile buffers
+    static const uint32_t wave[3] = {resident_ctas(k_compress<1>, kCompressWarps * 32, kSmem),
+                                     resident_ctas(k_compress<2>, kCompressWarps * 32, kSmem),
+                                     resident_ctas(k_compress<3>, kCompressWarps * 32, kSmem)};
     const uint32_t nct  = (uint32_t)cdiv(a.ntiles, kCompressWarps);
     const uint32_t ctas = std::min(nct, wave[a.ndim - 1]);
     switch (a.ndim) {
-    case 1: k_compress<1><<<ctas, kCompressWarps * 32, 0, s>>>(a); break;
-    case 2: k_compress<2><<<ctas, kCompressWarps * 32, 0, s>>>(a); break;
-    default: k_compress<3><<<ctas, kCompressWarps * 32, 0, s>>>(a); break;
+    case 1: k_compress<1><<<ctas, kCompressWarps * 32, kSmem, s>>>(a); break;
+    case 2: k_compress<2><<<ctas, kCompressWarps * 32, kSmem, s>>>(a); break;
+    default: k_compress<3><<<ctas, kCompressWarps * 32, kSmem, s>>>(a); break;
     }
     return cudaGetLastError();
 }
