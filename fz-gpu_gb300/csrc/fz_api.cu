@@ -667,7 +667,7 @@ fz_status fz_batch_create(fz_workspace* ws, const fz_field* fields, uint32_t cou
     cudaStream_t cs;
     cudaError_t  e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e != cudaSuccess) return map_err(e);
-    // no timing events inside a graph
+    // no timing events inside a graph (event-record nodes would serialise the replay)
     const uint32_t tcap = ws->tcap;
     ws->tcap            = 0;
     fz_batch* b         = new (std::nothrow) fz_batch();

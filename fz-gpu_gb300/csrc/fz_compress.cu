@@ -123,6 +123,70 @@ __device__ __forceinline__ void fast3d(const float* __restrict__ in, const Geo& 
     }
 }
 
+// Swizzled position (in u32 words) of 16-byte chunk q of a block's code image: chunk
+// (g, t) of group g lives at g*8 + (t ^ (g & 7)) so that both the row-major writes of
+// the Lorenzo phase and the per-group reads of the transpose are conflict-free.
+__device__ __forceinline__ uint32_t swz(uint32_t q)
+{
+    const uint32_t g = q >> 3, t = q & 7u;
+    return ((g << 3) | (t ^ (g & 7u))) << 2;
+}
+
+// A whole 2D shuffle block [base, base+2048) when every element lies inside x*y and rows
+// are a multiple of 4 elements long (so a group of 4 never straddles a row and halo rows
+// are 16-byte aligned).  Same float expressions as fast2d; the west neighbour's t of lane
+// 0 is carried from lane 31 of the previous group row, row/column advance incrementally,
+// and the next group's loads are issued before the current one is processed.
+__device__ __forceinline__ void block2d(const float* __restrict__ in, const Geo& g, uint32_t base, float r,
+                                        uint32_t lane, uint32_t* sm, uint32_t& ovf)
+{
+    uint32_t e0  = base + lane * 4;
+    uint32_t row = fdiv(e0, g.dx), col = e0 - row * g.x;
+    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4       v  = ldg4(in + e0);
+    float4       u  = (row & 15u) ? ldg4(in + (e0 - g.x)) : z4;
+    // t = c - n of element base-1, the west neighbour of lane 0's first group
+    float carry = 0.0f;
+    if (lane == 0 && (col & 15u))
+        carry = __fsub_rn(pq(__ldg(in + e0 - 1), r), (row & 15u) ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f);
+    bool ov = false;
+#pragma unroll 2
+    for (uint32_t it = 0; it < 16; ++it) {
+        const bool rin = (row & 15u) != 0, cin = (col & 15u) != 0;
+        // next group row of this lane: 128 elements on
+        uint32_t rown = row, coln = col + 128;
+        if (g.x >= 128) {
+            if (coln >= g.x) coln -= g.x, ++rown;
+        } else {
+            rown = fdiv(e0 + 128, g.dx), coln = e0 + 128 - rown * g.x;
+        }
+        float4 vn = z4, un = z4;
+        if (it < 15) {
+            vn = ldg4(in + e0 + 128);
+            if (rown & 15u) un = ldg4(in + (e0 + 128 - g.x));
+        }
+        float t[4];
+        t[0] = __fsub_rn(pq(v.x, r), rin ? pq(u.x, r) : 0.0f);
+        t[1] = __fsub_rn(pq(v.y, r), rin ? pq(u.y, r) : 0.0f);
+        t[2] = __fsub_rn(pq(v.z, r), rin ? pq(u.z, r) : 0.0f);
+        t[3] = __fsub_rn(pq(v.w, r), rin ? pq(u.w, r) : 0.0f);
+        const float up = __shfl_up_sync(kFull, t[3], 1);
+        const float tw = cin ? (lane ? up : carry) : 0.0f;
+        carry          = __shfl_sync(kFull, t[3], 31);
+        uint32_t c[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float d = __fsub_rn(t[j], j ? t[j - 1] : tw);
+            c[j]          = pack_signed(d);
+            ov |= !(fabsf(d) < 32768.0f);
+        }
+        const uint32_t q = it * 16 + (lane >> 1);
+        *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+        v = vn, u = un, row = rown, col = coln, e0 += 128;
+    }
+    ovf |= ov ? 1u : 0u;
+}
+
 template <int ND>
 __device__ __forceinline__ void codes4(const float* __restrict__ in, const Geo& g, uint32_t e0,
                                        float r, uint32_t lane, uint32_t (&code)[4],
@@ -326,14 +390,6 @@ __device__ void write_header(const CompressArgs& a, const EbInfo& e, uint32_t ov
     *reinterpret_cast<uint4*>(h + 48) = make_uint4(nnz, 0u, __float_as_uint(e.range), a.sidecar_bytes);
 }
 
-// Swizzled position (in u32 words) of 16-byte chunk q of a block's code image: chunk
-// (g, t) of group g lives at g*8 + (t ^ (g & 7)) so that both the row-major writes of
-// the Lorenzo phase and the per-group reads of the transpose are conflict-free.
-__device__ __forceinline__ uint32_t swz(uint32_t q)
-{
-    const uint32_t g = q >> 3, t = q & 7u;
-    return ((g << 3) | (t ^ (g & 7u))) << 2;
-}
 
 // Persistent: one resident wave of CTAs; each CTA repeatedly takes the next scan tile
 // (8 shuffle blocks, one per warp) from the ticket counter.  Tickets are handed out in
@@ -347,7 +403,7 @@ __device__ __forceinline__ uint32_t swz(uint32_t q)
 // published their inclusive prefixes, so its look-back is about one round trip instead
 // of a walk past every tile in flight.
 template <int ND>
-__global__ void __launch_bounds__(kCompressWarps * 32) k_compress(const CompressArgs a)
+__global__ void __launch_bounds__(kCompressWarps * 32, 3) k_compress(const CompressArgs a)
 {
     extern __shared__ __align__(16) uint32_t dsm[];  // [2][kCompressWarps][kBlockWords]
     __shared__ uint32_t s_cnt[2][kCompressWarps], s_ovf[2][kCompressWarps], s_tile[2], s_tot[2];
@@ -387,10 +443,13 @@ __global__ void __launch_bounds__(kCompressWarps * 32) k_compress(const Compress
             const uint32_t t    = ct * kCompressWarps + wid;  // this warp's shuffle block
             const uint32_t base = t * kBlockCodes;
             uint32_t       ovf  = 0, cnt = 0;
+            if (ND == 2 && t < a.nb && g.al_x && base + kBlockCodes <= g.nl) {
+                block2d(a.in, g, base, r, lane, sm, ovf);
+            }
             if (t < a.nb) {
                 // ---- phase A: codes of the block into shared memory (swizzled) ----
-#pragma unroll 2
-                for (uint32_t it = 0; it < 16; ++it) {
+#pragma unroll 4
+                for (uint32_t it = 0; it < ((ND == 2 && g.al_x && base + kBlockCodes <= g.nl) ? 0u : 16u); ++it) {
                     const uint32_t e0 = base + it * 128 + lane * 4;
                     uint32_t       c[4], sgn = 0;
                     codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
