@@ -51,6 +51,11 @@ def parse_args():
     p.add_argument("--impl", choices=["fz", "reference"], default="fz")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--workload", choices=["exafel", "batch", "serving"], default="exafel",
+                   help="exafel: the headline line; batch: configs[3]; serving: configs[4]")
+    p.add_argument("--batch-fields", type=int, default=512)
+    p.add_argument("--serve-seconds", type=float, default=3.0)
+    p.add_argument("--serve-rate", type=float, default=2000.0)
     return p.parse_args()
 
 
@@ -404,11 +409,170 @@ def e2e(fz, L, fields, n, cap, sizes, args, dev, world, dist):
             "d2h_bytes_per_step": int(per_step_stream + len(fields) * 4 * n)}
 
 
+def _torch_fields(specs, dev):
+    import importlib
+    import __graft_entry__ as g
+    g.load_package()
+    synth = importlib.import_module("fz_gpu_gb300.synth")
+    return [synth.field_torch(kind, dims, seed, device=dev) for kind, dims, _, seed in specs]
+
+
+def run_batch(args, local_rank):
+    """configs[3]: a mixed batch (log-uniform 64 KB-256 MB, 1D/2D/3D, eb from
+    {1e-2,1e-3,1e-4}) compressed and decompressed from two CUDA-graph replays, against the
+    plain per-field path (fz_compress with its size readback, then fz_decompress)."""
+    import importlib
+    import torch
+    import __graft_entry__ as g
+    fz = g.load_package()
+    synth = importlib.import_module("fz_gpu_gb300.synth")
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    specs = synth.mixed_specs(args.batch_fields, seed=3)
+    X = _torch_fields(specs, dev)
+    ns = [x.numel() for x in X]
+    caps = [fz.max_compressed_bytes(n, d) for n, (_, d, _, _) in zip(ns, specs)]
+    S = [torch.empty(c, dtype=torch.uint8, device=dev) for c in caps]
+    Y = [torch.empty(n, dtype=torch.float32, device=dev) for n in ns]
+    ws = fz.Workspace(max(ns))
+    total = 4 * sum(ns)
+    stream = torch.cuda.current_stream(dev)
+    # plain per-field path, as a caller handling one field at a time
+    def plain():
+        for x, s_, y, (_, d, eb, _) in zip(X, S, Y, specs):
+            st = fz.compress(x, d, eb, ws=ws, out=s_)
+            fz.decompress(st, ws=ws, out=y)
+    plain()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain()
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    heads = [fz.parse_header(s_[:64].cpu().numpy()) for s_ in S]
+    sizes = [fz.stream_bytes(h) for h in heads]
+    comp = fz.fields_array([{"src": x.data_ptr(), "dst": s_.data_ptr(), "n": n, "dims": d, "eb": eb,
+                             "dst_capacity": s_.numel()} for x, s_, n, (_, d, eb, _) in zip(X, S, ns, specs)])
+    dec = fz.fields_array([{"src": s_.data_ptr(), "dst": y.data_ptr(), "src_bytes": b, "dst_capacity": y.numel(),
+                            "header": h} for s_, y, b, h in zip(S, Y, sizes, heads)])
+    gc, gd = fz.Batch(ws, comp, fz.COMPRESS), fz.Batch(ws, dec, fz.DECOMPRESS)
+    for _ in range(2):
+        gc.launch(stream), gd.launch(stream)
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 5))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        gc.launch(stream), gd.launch(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_batch = e0.elapsed_time(e1) / 1e3 / steps
+    # every stream of the replays equals the plain path's (which tests check bit for bit)
+    assert all(fz.parse_header(s_[:64].cpu().numpy()).nnz == h.nnz for s_, h in zip(S[:8], heads[:8]))
+    ratio = sum(4 * n for n in ns) / sum(sizes)
+    line = {"metric": "configs[3]: batched vs per-field aggregate GB/s (compress + decompress)",
+            "value": round(2 * total / t_batch / 1e9, 2), "unit": "GB/s",
+            "per_field_plain": round(2 * total / t_plain / 1e9, 2),
+            "speedup_vs_per_field": round(t_plain / t_batch, 2),
+            "fields": len(specs), "total_gb": round(total / 1e9, 3), "steps": steps,
+            "aggregate_ratio": round(ratio, 3), "higher_is_better": True,
+            "data": "synthetic (seeded device-side generators)",
+            "config": {"workload": "mixed 1D/2D/3D, sizes log-uniform 64 KB-256 MB, eb in {1e-2,1e-3,1e-4}",
+                       "batched": "two CUDA-graph replays (fz_batch_launch)",
+                       "per_field": "fz_compress with size readback + fz_decompress, one field at a time"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args, local_rank):
+    """configs[4]: Poisson arrivals (mean --serve-rate req/s) of fields drawn as in
+    configs[3], 60/40 compress/decompress, host buffers; the request loop with 8 slots and
+    an HBM budget against the same trace served one request at a time (1 slot)."""
+    import importlib
+    import numpy as np
+    import torch
+    import __graft_entry__ as g
+    fz = g.load_package()
+    synth = importlib.import_module("fz_gpu_gb300.synth")
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    specs = synth.mixed_specs(48, seed=4)
+    Xd = _torch_fields(specs, dev)
+    ns = [x.numel() for x in Xd]
+    ws = fz.Workspace(max(ns))
+    hin, hst, hout_c, hout_d, sbytes = [], [], [], [], []
+    for x, (_, d, eb, _) in zip(Xd, specs):
+        st = fz.compress(x, d, eb, ws=ws)
+        hin.append(x.cpu().pin_memory())
+        hst.append(st.cpu().pin_memory())
+        sbytes.append(st.numel())
+        hout_c.append(torch.empty(fz.max_compressed_bytes(x.numel(), d), dtype=torch.uint8).pin_memory())
+        hout_d.append(torch.empty(x.numel(), dtype=torch.float32).pin_memory())
+    del Xd
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(4)
+    nreq = int(args.serve_rate * args.serve_seconds)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, nreq))
+    fields = rng.integers(0, len(specs), nreq)
+    comp = rng.random(nreq) < 0.6
+    free = torch.cuda.mem_get_info(dev)[0]
+    budget = int(min(120 << 30, free - (16 << 30)))
+
+    def serve(slots, trace=True):
+        server = fz.Server(budget, slots, max(ns))
+        lat = np.zeros(nreq)
+        t0 = time.perf_counter()
+        i, done, last = 0, 0, 0.0
+        while done < nreq:
+            now = time.perf_counter() - t0
+            while i < nreq and (not trace or arrivals[i] <= now):
+                f = int(fields[i])
+                _, d, eb, _ = specs[f]
+                if comp[i]:
+                    server.submit(i, fz.COMPRESS, hin[f].data_ptr(), hout_c[f].data_ptr(), hout_c[f].numel(),
+                                  n=ns[f], dims=d, eb=eb)
+                else:
+                    server.submit(i, fz.DECOMPRESS, hst[f].data_ptr(), hout_d[f].data_ptr(), 4 * ns[f],
+                                  src_bytes=sbytes[f])
+                i += 1
+            for rid, st, _ in server.poll():
+                if st != fz.SUCCESS:
+                    raise fz.FzError("serving", st)
+                now = time.perf_counter() - t0
+                lat[rid] = now - (arrivals[rid] if trace else 0.0)
+                last = max(last, now)
+                done += 1
+        server.close()
+        moved = float(sum(4 * ns[int(f)] for f in fields))
+        return lat, moved / last / 1e9
+
+    lat8, gbs8 = serve(8)
+    lat1, gbs1 = serve(1)
+    sat8 = serve(8, trace=False)[1]
+    sat1 = serve(1, trace=False)[1]
+    pct = lambda a: {"p50_ms": round(1e3 * float(np.percentile(a, 50)), 3),
+                     "p99_ms": round(1e3 * float(np.percentile(a, 99)), 3),
+                     "p99.9_ms": round(1e3 * float(np.percentile(a, 99.9)), 3)}
+    line = {"metric": "configs[4]: served latency and aggregate GB/s (uncompressed bytes)",
+            "requests": nreq, "rate_req_s": args.serve_rate, "hbm_budget_gb": round(budget / 2 ** 30, 1),
+            "served": dict(slots=8, gbs=round(gbs8, 2), **pct(lat8)),
+            "one_at_a_time": dict(slots=1, gbs=round(gbs1, 2), **pct(lat1)),
+            "saturated_gbs": {"slots8": round(sat8, 2), "slots1": round(sat1, 2),
+                              "speedup": round(sat8 / sat1, 2)},
+            "data": "synthetic (seeded device-side generators, 48 distinct fields, host pinned buffers)",
+            "config": {"workload": "Poisson arrivals, 60/40 compress/decompress, fields as configs[3]"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     rank, world, local_rank = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "batch":
+        if rank == 0:
+            run_batch(args, local_rank)
+    elif args.workload == "serving":
+        if rank == 0:
+            run_serving(args, local_rank)
     else:
         run_fz(args, rank, world, local_rank)
 

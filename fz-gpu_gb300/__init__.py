@@ -64,6 +64,16 @@ class Field(C.Structure):
 
 COMPRESS, DECOMPRESS = 0, 1
 
+
+class Request(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("dir", C.c_int), ("src", C.c_void_p), ("dst", C.c_void_p),
+                ("n", C.c_uint64), ("dims", Dims), ("eb", C.c_double), ("eb_mode", C.c_int),
+                ("mode", C.c_int), ("dst_capacity", C.c_uint64), ("src_bytes", C.c_uint64)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("status", C.c_int), ("bytes", C.c_uint64)]
+
 _lock = threading.Lock()
 _lib = None
 
@@ -99,6 +109,11 @@ SIGNATURES = {
     "fz_batch_create": (_I, [_P, _P, _U32, _I, _I, _I, C.POINTER(_P)]),
     "fz_batch_launch": (_I, [_P, _P]),
     "fz_batch_destroy": (_I, [_P]),
+    "fz_server_create": (_I, [_U64, _U32, _U64, C.POINTER(_P)]),
+    "fz_server_submit": (_I, [_P, C.POINTER(Request)]),
+    "fz_server_poll": (_I, [_P, C.POINTER(Completion), _U32, C.POINTER(C.c_uint32)]),
+    "fz_server_pending": (_I, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), _PU64]),
+    "fz_server_destroy": (_I, [_P]),
 }
 
 
@@ -399,6 +414,46 @@ class Batch:
     def close(self):
         if self.handle:
             lib().fz_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------ serving
+class Server:
+    """Request loop with continuous batching under an HBM budget (fz_server_*).
+    Requests use host buffers; keep them alive until their completion is polled."""
+
+    def __init__(self, hbm_budget, slots, max_n):
+        h = C.c_void_p()
+        _check("fz_server_create", lib().fz_server_create(int(hbm_budget), int(slots), int(max_n), C.byref(h)))
+        self.handle = h
+        self._out = (Completion * 256)()
+
+    def submit(self, rid, direction, src, dst, dst_capacity, n=0, dims=(1, 1, 1), eb=0.0, rel=True,
+               mode=MODE_SIDECAR, src_bytes=0):
+        r = Request(int(rid), int(direction), src, dst, int(n), _dims(dims), float(eb),
+                    EB_REL if rel else EB_ABS, int(mode), int(dst_capacity), int(src_bytes))
+        _check("fz_server_submit", lib().fz_server_submit(self.handle, C.byref(r)))
+
+    def poll(self):
+        """Retire finished requests and admit queued ones; returns [(id, status, bytes)]."""
+        cnt = C.c_uint32()
+        _check("fz_server_poll", lib().fz_server_poll(self.handle, self._out, 256, C.byref(cnt)))
+        return [(self._out[i].id, self._out[i].status, self._out[i].bytes) for i in range(cnt.value)]
+
+    def pending(self):
+        q, r, u = C.c_uint32(), C.c_uint32(), C.c_uint64()
+        _check("fz_server_pending", lib().fz_server_pending(self.handle, C.byref(q), C.byref(r), C.byref(u)))
+        return q.value, r.value, u.value
+
+    def close(self):
+        if self.handle:
+            lib().fz_server_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

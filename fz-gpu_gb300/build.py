@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfzgb300.so")
 CLI = os.path.join(HERE, "fz-gpu")
 
-CU_SOURCES = ["fz_compress.cu", "fz_decompress.cu", "fz_api.cu", "fz_noalloc.cu"]
+CU_SOURCES = ["fz_compress.cu", "fz_decompress.cu", "fz_api.cu", "fz_noalloc.cu", "fz_server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-O3",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]

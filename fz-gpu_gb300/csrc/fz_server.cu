@@ -1,0 +1,314 @@
+// fz_server.cu -- a request loop that compresses and decompresses fields as they
+// arrive, with continuous batching under an HBM budget.
+//
+// The server owns
+//   * a device pool of `hbm_budget` bytes (one allocation, first-fit free list with
+//     coalescing) from which each admitted request takes its input and output buffers;
+//   * `slots` execution slots, each a CUDA stream with its own workspace (scan state),
+//     a pinned 128-byte readback buffer and two events.
+// Requests (host buffers; pinned ones let the copies overlap) wait in a FIFO.
+// fz_server_poll never blocks: it retires requests whose work has finished, then admits
+// queued requests while a slot is free and the pool can hold their buffers.  Requests
+// on different slots overlap on the device (copies on the copy engines, kernels
+// side by side), so work that arrives while others run starts as soon as memory and a
+// slot free up.
+#include <cstring>
+#include <deque>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "../../include/fz.h"
+#include "fz_internal.h"
+#include "fz_workspace.h"
+
+using namespace fz;
+
+namespace {
+
+// First-fit allocator over [0, size) with 256-byte granules; frees coalesce.
+class Pool {
+public:
+    explicit Pool(uint64_t size) { free_[0] = size; }
+    bool alloc(uint64_t bytes, uint64_t* off)
+    {
+        bytes = (bytes + 255) & ~uint64_t(255);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second < bytes) continue;
+            *off              = it->first;
+            const uint64_t rest = it->second - bytes, at = it->first + bytes;
+            free_.erase(it);
+            if (rest) free_[at] = rest;
+            used_ += bytes;
+            return true;
+        }
+        return false;
+    }
+    void release(uint64_t off, uint64_t bytes)
+    {
+        bytes = (bytes + 255) & ~uint64_t(255);
+        used_ -= bytes;
+        auto it = free_.emplace(off, bytes).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    uint64_t used() const { return used_; }
+
+private:
+    std::map<uint64_t, uint64_t> free_;
+    uint64_t                     used_ = 0;
+};
+
+enum class Phase { Idle, WaitHeader, WaitDone };
+
+struct Slot {
+    cudaStream_t  stream = nullptr;
+    fz_workspace* ws     = nullptr;
+    uint8_t*      h_buf  = nullptr;  // pinned: header (64 B) + status word
+    cudaEvent_t   ev     = nullptr;
+    Phase         phase  = Phase::Idle;
+    fz_request    req{};
+    uint64_t      src_off = 0, src_bytes = 0, dst_off = 0, dst_bytes = 0;
+    uint64_t      result  = 0;
+    fz_status     status  = FZ_SUCCESS;
+};
+
+uint64_t max_stream_bytes(uint64_t n, fz_dims d, fz_mode m)
+{
+    uint64_t b = 0;
+    return fz_max_compressed_bytes(n, d, m, &b) == FZ_SUCCESS ? b : 0;
+}
+
+}  // namespace
+
+struct fz_server {
+    uint8_t*                   d_pool = nullptr;
+    Pool*                      pool   = nullptr;
+    uint64_t                   budget = 0, max_n = 0;
+    std::vector<Slot>          slots;
+    std::deque<fz_request>     queue;
+    std::deque<fz_completion>  done;  // finished but not yet handed out
+};
+
+namespace {
+
+bool request_bytes(const fz_request& r, uint64_t* src, uint64_t* dst)
+{
+    if (r.dir == FZ_COMPRESS) {
+        *src = 4 * r.n;
+        *dst = max_stream_bytes(r.n, r.dims, r.mode);
+        return *dst != 0;
+    }
+    fz_header h;
+    std::memcpy(&h, r.src, sizeof(h));
+    *src = r.src_bytes;
+    *dst = 4 * h.n;
+    return true;
+}
+
+void finish(fz_server* S, Slot& sl, fz_status st, uint64_t result)
+{
+    S->pool->release(sl.src_off, sl.src_bytes);
+    S->pool->release(sl.dst_off, sl.dst_bytes);
+    S->done.push_back(fz_completion{sl.req.id, st, result});
+    sl.phase = Phase::Idle;
+}
+
+// Enqueues a request's copies and kernels on a free slot.
+void issue(fz_server* S, Slot& sl, const fz_request& r, uint64_t src_off, uint64_t src_b, uint64_t dst_off,
+           uint64_t dst_b)
+{
+    sl.req = r, sl.src_off = src_off, sl.src_bytes = src_b, sl.dst_off = dst_off, sl.dst_bytes = dst_b;
+    uint8_t*    d_src = S->d_pool + src_off;
+    uint8_t*    d_dst = S->d_pool + dst_off;
+    fz_stream_t hs    = reinterpret_cast<fz_stream_t>(sl.stream);
+    cudaError_t e     = cudaMemcpyAsync(d_src, r.src, src_b, cudaMemcpyHostToDevice, sl.stream);
+    fz_status   st    = e == cudaSuccess ? FZ_SUCCESS : FZ_FAIL_GPU_MEMCPY;
+    if (r.dir == FZ_COMPRESS) {
+        if (st == FZ_SUCCESS)
+            st = fz_compress(sl.ws, reinterpret_cast<const float*>(d_src), r.n, r.dims, r.eb, r.eb_mode, r.mode,
+                             d_dst, dst_b, nullptr, hs);
+        // header and status come back first; the stream's length follows from nnz
+        if (st == FZ_SUCCESS && cudaMemcpyAsync(sl.h_buf, d_dst, 64, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+            st = FZ_FAIL_GPU_MEMCPY;
+        if (st == FZ_SUCCESS && cudaMemcpyAsync(sl.h_buf + 64, sl.ws->status, 4, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+            st = FZ_FAIL_GPU_MEMCPY;
+        sl.phase = Phase::WaitHeader;
+    } else {
+        fz_header h;
+        std::memcpy(&h, r.src, sizeof(h));
+        if (st == FZ_SUCCESS)
+            st = fz_decompress(sl.ws, d_src, r.src_bytes, &h, reinterpret_cast<float*>(d_dst), h.n, hs);
+        if (st == FZ_SUCCESS && cudaMemcpyAsync(r.dst, d_dst, 4 * h.n, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+            st = FZ_FAIL_GPU_MEMCPY;
+        if (st == FZ_SUCCESS && cudaMemcpyAsync(sl.h_buf + 64, sl.ws->status, 4, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+            st = FZ_FAIL_GPU_MEMCPY;
+        sl.result = h.n;
+        sl.phase  = Phase::WaitDone;
+    }
+    if (st == FZ_SUCCESS && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
+    if (st != FZ_SUCCESS) {
+        cudaStreamSynchronize(sl.stream);
+        finish(S, sl, st, 0);
+    }
+}
+
+fz_status status_word(const Slot& sl)
+{
+    uint32_t w;
+    std::memcpy(&w, sl.h_buf + 64, 4);
+    if (w & kStatusTimeout) return FZ_TIMEOUT;
+    if (w & kStatusNonfinite) return FZ_NONFINITE_INPUT;
+    if (w & kStatusCorrupt) return FZ_CORRUPT_STREAM;
+    return FZ_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+fz_status fz_server_create(uint64_t hbm_budget, uint32_t slots, uint64_t max_n, fz_server** out)
+{
+    if (!out || !hbm_budget || !slots || slots > 64 || !max_n) return FZ_INVALID_ARG;
+    *out        = nullptr;
+    fz_server* S = new (std::nothrow) fz_server();
+    if (!S) return FZ_FAIL_GPU_MALLOC;
+    S->budget = hbm_budget, S->max_n = max_n;
+    if (cudaMalloc((void**)&S->d_pool, hbm_budget) != cudaSuccess) {
+        delete S;
+        return FZ_FAIL_GPU_OUT_OF_MEMORY;
+    }
+    S->pool = new Pool(hbm_budget);
+    S->slots.resize(slots);
+    for (Slot& sl : S->slots) {
+        fz_status st = fz_workspace_create(max_n, &sl.ws);
+        if (st == FZ_SUCCESS && cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess)
+            st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
+        if (st == FZ_SUCCESS && cudaMallocHost((void**)&sl.h_buf, 128) != cudaSuccess) st = FZ_FAIL_GPU_MALLOC;
+        if (st == FZ_SUCCESS && cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess)
+            st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
+        if (st != FZ_SUCCESS) {
+            fz_server_destroy(S);
+            return st;
+        }
+    }
+    *out = S;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_server_submit(fz_server* S, const fz_request* r)
+{
+    if (!S || !r || !r->src || !r->dst) return FZ_INVALID_ARG;
+    if (r->dir != FZ_COMPRESS && r->dir != FZ_DECOMPRESS) return FZ_INVALID_ARG;
+    if (r->dir == FZ_DECOMPRESS && r->src_bytes < FZ_HEADER_BYTES) return FZ_INVALID_ARG;
+    S->queue.push_back(*r);
+    return FZ_SUCCESS;
+}
+
+fz_status fz_server_poll(fz_server* S, fz_completion* out, uint32_t max, uint32_t* count)
+{
+    if (!S || !count || (!out && max)) return FZ_INVALID_ARG;
+    // retire
+    for (Slot& sl : S->slots) {
+        if (sl.phase == Phase::Idle) continue;
+        const cudaError_t q = cudaEventQuery(sl.ev);
+        if (q == cudaErrorNotReady) continue;
+        if (q != cudaSuccess) {
+            finish(S, sl, FZ_FAIL_GPU_ILLEGAL_ACCESS, 0);
+            continue;
+        }
+        if (sl.phase == Phase::WaitHeader) {
+            fz_header h;
+            std::memcpy(&h, sl.h_buf, sizeof(h));
+            uint64_t  bytes = 0;
+            fz_status st    = status_word(sl);
+            if (st == FZ_SUCCESS) st = fz_stream_bytes(&h, &bytes);
+            if (st == FZ_SUCCESS && bytes > sl.req.dst_capacity) st = FZ_OUT_OF_SPACE;
+            if (st == FZ_SUCCESS &&
+                cudaMemcpyAsync(sl.req.dst, S->d_pool + sl.dst_off, bytes, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+                st = FZ_FAIL_GPU_MEMCPY;
+            if (st == FZ_SUCCESS && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
+            if (st != FZ_SUCCESS) {
+                finish(S, sl, st, 0);
+                continue;
+            }
+            sl.result = bytes;
+            sl.phase  = Phase::WaitDone;
+            continue;
+        }
+        finish(S, sl, sl.req.dir == FZ_DECOMPRESS ? status_word(sl) : FZ_SUCCESS, sl.result);
+    }
+    // admit, first come first served
+    while (!S->queue.empty()) {
+        Slot* free_slot = nullptr;
+        for (Slot& sl : S->slots)
+            if (sl.phase == Phase::Idle) {
+                free_slot = &sl;
+                break;
+            }
+        if (!free_slot) break;
+        const fz_request r = S->queue.front();
+        uint64_t         sb = 0, db = 0;
+        const uint64_t   n  = r.dir == FZ_COMPRESS ? r.n : reinterpret_cast<const fz_header*>(r.src)->n;
+        const bool small_dst = r.dir == FZ_DECOMPRESS && 4 * n > r.dst_capacity;
+        if (!request_bytes(r, &sb, &db) || n > S->max_n || small_dst || sb + db + 512 > S->budget) {
+            S->queue.pop_front();  // can never run
+            S->done.push_back(fz_completion{r.id, n > S->max_n ? FZ_INVALID_ARG : FZ_OUT_OF_SPACE, 0});
+            continue;
+        }
+        uint64_t so = 0, dof = 0;
+        if (!S->pool->alloc(sb, &so)) break;  // wait for memory to free up
+        if (!S->pool->alloc(db, &dof)) {
+            S->pool->release(so, sb);
+            break;
+        }
+        S->queue.pop_front();
+        issue(S, *free_slot, r, so, sb, dof, db);
+    }
+    uint32_t k = 0;
+    while (k < max && !S->done.empty()) {
+        out[k++] = S->done.front();
+        S->done.pop_front();
+    }
+    *count = k;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_server_pending(fz_server* S, uint32_t* queued, uint32_t* running, uint64_t* pool_used)
+{
+    if (!S) return FZ_INVALID_ARG;
+    uint32_t r = 0;
+    for (const Slot& sl : S->slots) r += sl.phase != Phase::Idle;
+    if (queued) *queued = (uint32_t)S->queue.size();
+    if (running) *running = r;
+    if (pool_used) *pool_used = S->pool->used();
+    return FZ_SUCCESS;
+}
+
+fz_status fz_server_destroy(fz_server* S)
+{
+    if (!S) return FZ_INVALID_ARG;
+    for (Slot& sl : S->slots) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        if (sl.ws) fz_workspace_destroy(sl.ws);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+        if (sl.h_buf) cudaFreeHost(sl.h_buf);
+        if (sl.ev) cudaEventDestroy(sl.ev);
+    }
+    cudaFree(S->d_pool);
+    delete S->pool;
+    delete S;
+    return FZ_SUCCESS;
+}
+
+}  // extern "C"

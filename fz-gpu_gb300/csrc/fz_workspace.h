@@ -1,0 +1,33 @@
+// fz_workspace.h -- the workspace behind the opaque fz_workspace handle (internal).
+#pragma once
+
+#include <vector>
+
+#include "fz_internal.h"
+
+struct fz_workspace {
+    int       device;
+    uint64_t  max_n;
+    uint32_t  max_tiles;
+    void*     d_base;
+    size_t    d_bytes;
+    uint64_t* state;
+    uint32_t* tickets;  // [0] compress, [1] offsets, [2] scan-encode
+    uint32_t* status;
+    uint32_t* total;
+    uint32_t* epoch;    // device epoch of the scan state
+    uint32_t* mm;       // range accumulators (min, max as ordered u32)
+    uint16_t* codes;
+    uint32_t* boff;     // chunk offset of each shuffle block (decompression)
+    uint8_t*  h_pinned;  // 64-byte header + status word
+    // host-buffer path staging, allocated on first use
+    float*    d_field;
+    uint8_t*  d_stream;
+    uint64_t  stream_cap;
+    // per-kernel timing ring (fz_workspace_enable_timing)
+    std::vector<cudaEvent_t> tev;   // 2 per record
+    std::vector<int>         tkind;
+    uint32_t                 tcap  = 0;
+    uint32_t                 tused = 0;
+};
+

@@ -128,3 +128,80 @@ CONFIGS = [
     ("exafel-like 39200x388", "peaks2d", (39200, 388, 1), 1, (1e-3, 1e-4)),
     ("hurricane-like 500x500x100", "smooth3d", (500, 500, 100), 2, (1e-2, 1e-3, 1e-4)),
 ]
+
+
+# ------------------------------------------------------------------ mixed batches
+def _dims_for(n, nd, rng):
+    """Dims with x*y*z <= n close to n for a 1D/2D/3D field of about n elements."""
+    if nd == 1:
+        return (n, 1, 1)
+    if nd == 2:
+        x = max(2, int(round(math.sqrt(n * rng.uniform(0.5, 4.0)))))
+        return (x, max(2, n // x), 1)
+    s = max(2, int(round(n ** (1 / 3))))
+    return (s, s, max(2, n // (s * s)))
+
+
+def mixed_specs(count, seed=3, lo_bytes=64 << 10, hi_bytes=256 << 20, ebs=(1e-2, 1e-3, 1e-4)):
+    """configs[3]/[4]: `count` fields with sizes log-uniform between 64 KB and 256 MB,
+    mixed 1D/2D/3D, each with an eb drawn from {1e-2, 1e-3, 1e-4}.  Returns
+    [(kind, dims, eb, seed)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        nbytes = math.exp(rng.uniform(math.log(lo_bytes), math.log(hi_bytes)))
+        n = max(64, int(nbytes // 4))
+        nd = int(rng.integers(1, 4))
+        dims = _dims_for(n, nd, rng)
+        kind = {1: "smooth1d", 2: "smooth2d" if rng.random() < 0.6 else "peaks2d", 3: "smooth3d"}[nd]
+        out.append((kind, dims, float(ebs[int(rng.integers(0, len(ebs)))]), seed * 100000 + i))
+    return out
+
+
+def field_torch(kind, dims, seed, device="cuda"):
+    """Device-side generator of the same field families (sums of separable sinusoids with
+    zero patches, or Gaussian peaks on a noisy background), for multi-GB batches.  It
+    is not bit-identical to the numpy generators, only alike in distribution."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    x, y, z = dims
+    f32 = torch.float32
+
+    def U(*shape, lo=0.0, hi=1.0):
+        return lo + (hi - lo) * torch.rand(*shape, generator=g, device=device, dtype=f32)
+
+    if kind == "smooth1d":
+        t = torch.arange(x * y * z, device=device, dtype=f32)
+        f = torch.zeros_like(t)
+        for _ in range(6):
+            lam = torch.exp(U(1, lo=math.log(30.0), hi=math.log(5000.0)))
+            f += U(1, lo=0.2) * torch.sin(2 * math.pi * t / lam + U(1, hi=6.28))
+        f = (f - f.min()) / (f.max() - f.min() + 1e-30)
+        f[f < 0.1] = 0
+        return f
+    if kind == "peaks2d":
+        f = 0.5 * torch.randn(y, x, generator=g, device=device, dtype=f32)
+        npk = max(1, int(2000 * x * y / (39200 * 388)))
+        cx, cy = U(npk, hi=float(x)), U(npk, hi=float(y))
+        amp = torch.exp(U(npk, lo=math.log(10.0), hi=math.log(1e4)))
+        ix = cx.long().clamp(0, x - 1)
+        iy = cy.long().clamp(0, y - 1)
+        f[iy, ix] += amp  # point sources, then a 3x3 blur gives sigma ~1 px peaks
+        f = torch.nn.functional.avg_pool2d(f[None, None], 3, 1, 1)[0, 0] * 9 / 4
+        return f.reshape(-1).contiguous()
+    # smooth2d / smooth3d: separable products of sinusoids
+    zs = torch.arange(z, device=device, dtype=f32)[:, None, None]
+    ys = torch.arange(y, device=device, dtype=f32)[None, :, None]
+    xs = torch.arange(x, device=device, dtype=f32)[None, None, :]
+    f = torch.zeros(z, y, x, device=device, dtype=f32)
+    for _ in range(8):
+        lx, ly, lz = torch.exp(U(3, lo=math.log(20.0), hi=math.log(800.0)))
+        ph = U(3, hi=6.28)
+        term = torch.sin(2 * math.pi * xs / lx + ph[0]) * torch.sin(2 * math.pi * ys / ly + ph[1])
+        if z > 1:
+            term = term * torch.sin(2 * math.pi * zs / lz + ph[2])
+        f += U(1, lo=0.2) * term
+    thr = torch.quantile(f.reshape(-1)[:: max(1, f.numel() // 65536)], 0.35)
+    f = torch.clamp(f - thr, min=0)
+    return f.reshape(-1).contiguous()

@@ -273,6 +273,46 @@ fz_status fz_batch_create(fz_workspace* ws, const fz_field* fields, uint32_t cou
 fz_status fz_batch_launch(fz_batch* batch, fz_stream_t stream);
 fz_status fz_batch_destroy(fz_batch* batch);
 
+/* -------------------------------------------------------------- serving -- */
+/* A request on host buffers (pinned buffers let copies overlap with other requests).
+   Compression: src float[n] with dims, eb, eb_mode, mode -> dst (dst_capacity bytes).
+   Decompression: src the stream (src_bytes; its header is read from src) -> dst float[n]
+   (dst_capacity bytes, at least 4n).  A request that can never run (larger than the
+   budget or than max_n, or dst too small) completes with FZ_OUT_OF_SPACE/FZ_INVALID_ARG. */
+typedef struct fz_request {
+    uint64_t     id;           /* the caller's tag, echoed in the completion */
+    fz_direction dir;
+    const void*  src;
+    void*        dst;
+    uint64_t     n;
+    fz_dims      dims;
+    double       eb;
+    fz_eb_mode   eb_mode;
+    fz_mode      mode;
+    uint64_t     dst_capacity;
+    uint64_t     src_bytes;
+} fz_request;
+
+typedef struct fz_completion {
+    uint64_t  id;
+    fz_status status;
+    uint64_t  bytes; /* compression: stream bytes written to dst; decompression: elements */
+} fz_completion;
+
+/* A request loop with continuous batching under an HBM budget: `slots` streams, each with
+   its own workspace, share one device pool of hbm_budget bytes from which every admitted
+   request takes its input and output buffers.  Requests queue in arrival order;
+   fz_server_poll (non-blocking) retires finished requests and admits queued ones as
+   slots and pool memory free up, so requests that arrive while others run overlap on
+   the device.  No counterpart in the reference (one field per process, fz.cu:226-238). */
+typedef struct fz_server fz_server;
+fz_status fz_server_create(uint64_t hbm_budget, uint32_t slots, uint64_t max_n, fz_server** out);
+fz_status fz_server_submit(fz_server* server, const fz_request* request);
+fz_status fz_server_poll(fz_server* server, fz_completion* out, uint32_t max, uint32_t* count);
+fz_status fz_server_pending(fz_server* server, uint32_t* queued, uint32_t* running,
+                            uint64_t* pool_used);
+fz_status fz_server_destroy(fz_server* server);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,69 @@
+"""The request loop (fz_server_*): every result is the same alone and in the mix, with
+requests overlapping on the device and waiting for HBM budget."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _fields(synth):
+    return [(synth.smooth2d(900, 400, seed=41), (900, 400, 1), 1e-3),
+            (synth.peaks2d(3000, 257, seed=42, npeaks=50), (3000, 257, 1), 1e-4),
+            (synth.smooth3d(70, 60, 50, seed=43), (70, 60, 50), 1e-3),
+            (synth.smooth1d(333333, seed=44), (333333, 1, 1), 1e-2),
+            (synth.smooth2d(64, 64, seed=45), (64, 64, 1), 1e-3),
+            (synth.smooth3d(33, 17, 9, seed=46), (33, 17, 9), 1e-4)]
+
+
+def _run(fz, server, reqs):
+    """Submit all, poll until every request has completed; returns {id: (status, bytes)}."""
+    for r in reqs:
+        server.submit(**r)
+    done = {}
+    while len(done) < len(reqs):
+        for rid, st, nb in server.poll():
+            done[rid] = (st, nb)
+    return done
+
+
+@pytest.mark.parametrize("budget_mb,slots", [(512, 4), (24, 2)])
+def test_results_identical_alone_and_in_the_mix(fz, synth, budget_mb, slots):
+    items = _fields(synth)
+    ws = fz.Workspace(max(d.size for d, _, _ in items))
+    alone = [fz.compress_host(d, dims, eb, ws=ws) for d, dims, eb in items]
+    alone_rec = [fz.decompress_host(s, ws=ws) for s in alone]
+    hin = [torch.from_numpy(d).pin_memory() for d, _, _ in items]
+    caps = [fz.max_compressed_bytes(d.size, dims) for d, dims, _ in items]
+    hout = [torch.empty(c, dtype=torch.uint8).pin_memory() for c in caps]
+    hst = [torch.from_numpy(s.copy()).pin_memory() for s in alone]
+    hrec = [torch.empty(d.size, dtype=torch.float32).pin_memory() for d, _, _ in items]
+    reqs = []
+    for i, (d, dims, eb) in enumerate(items):  # interleave compress and decompress requests
+        reqs.append(dict(rid=2 * i, direction=fz.COMPRESS, src=hin[i].data_ptr(), dst=hout[i].data_ptr(),
+                         dst_capacity=caps[i], n=d.size, dims=dims, eb=eb))
+        reqs.append(dict(rid=2 * i + 1, direction=fz.DECOMPRESS, src=hst[i].data_ptr(), dst=hrec[i].data_ptr(),
+                         dst_capacity=4 * d.size, src_bytes=alone[i].size))
+    server = fz.Server(budget_mb << 20, slots, max(d.size for d, _, _ in items))
+    done = _run(fz, server, reqs)
+    for i, (d, _, _) in enumerate(items):
+        st, nb = done[2 * i]
+        assert st == fz.SUCCESS and nb == alone[i].size
+        assert np.array_equal(hout[i][:nb].numpy(), alone[i])
+        st, nb = done[2 * i + 1]
+        assert st == fz.SUCCESS and nb == d.size
+        assert np.array_equal(hrec[i].numpy().view(np.uint32), alone_rec[i].view(np.uint32))
+    q, r, used = server.pending()
+    assert (q, r, used) == (0, 0, 0)
+    server.close()
+
+
+def test_request_larger_than_the_budget_is_rejected(fz, synth):
+    d = synth.smooth2d(600, 600, seed=47)
+    h = torch.from_numpy(d).pin_memory()
+    out = torch.empty(fz.max_compressed_bytes(d.size, (600, 600, 1)), dtype=torch.uint8).pin_memory()
+    server = fz.Server(1 << 20, 2, d.size)  # 1 MiB cannot hold a 1.44 MB field
+    done = _run(fz, server, [dict(rid=7, direction=fz.COMPRESS, src=h.data_ptr(), dst=out.data_ptr(),
+                                  dst_capacity=out.numel(), n=d.size, dims=(600, 600, 1), eb=1e-3)])
+    assert done[7][0] == fz.OUT_OF_SPACE
+    server.close()
