@@ -1,5 +1,6 @@
 // fz_api.cu -- the C ABI (include/fz.h): argument checks, stream layout, workspace,
 // and the launch sequences of the full pipeline and of the stage-level drop-ins.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -628,44 +629,78 @@ fz_status fz_decompress_batch(fz_workspace* ws, const fz_field* fields, uint32_t
 }  // extern "C"
 
 struct fz_batch {
-    cudaGraph_t     graph = nullptr;
-    cudaGraphExec_t exec  = nullptr;
+    cudaGraph_t                graph = nullptr;
+    cudaGraphExec_t            exec  = nullptr;
+    std::vector<fz_workspace*> own_ws;  // the extra branches' workspaces
 };
 
 extern "C" {
+
+// The batch is captured with parallel branches: fields go round-robin to up to
+// kBatchBranches forked streams, each with its own workspace (scan state, range
+// accumulators), so the kernels of small fields run side by side.
+static constexpr uint32_t kBatchBranches = 8;
 
 fz_status fz_batch_create(fz_workspace* ws, const fz_field* fields, uint32_t count, fz_direction dir,
                           fz_eb_mode eb_mode, fz_mode mode, fz_batch** out)
 {
     if (!ws || !out || (!fields && count) || (dir != FZ_COMPRESS && dir != FZ_DECOMPRESS)) return FZ_INVALID_ARG;
     *out = nullptr;
-    cudaStream_t cs;
-    cudaError_t  e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return map_err(e);
-    // no timing events inside a graph (event-record nodes would serialise the replay)
-    const uint32_t tcap = ws->tcap;
-    ws->tcap            = 0;
-    fz_batch* b         = new (std::nothrow) fz_batch();
-    fz_status st        = b ? FZ_SUCCESS : FZ_FAIL_GPU_MALLOC;
-    if (st == FZ_SUCCESS) {
-        e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-        if (e != cudaSuccess) st = map_err(e);
+    fz_batch* b = new (std::nothrow) fz_batch();
+    if (!b) return FZ_FAIL_GPU_MALLOC;
+    const uint32_t branches = std::max(1u, std::min(kBatchBranches, count));
+    uint64_t       max_n    = 1;
+    for (uint32_t i = 0; i < count; ++i) max_n = std::max<uint64_t>(max_n, dir == FZ_COMPRESS ? fields[i].n : fields[i].header.n);
+    std::vector<fz_workspace*> wss{ws};
+    fz_status                  st = FZ_SUCCESS;
+    for (uint32_t i = 1; i < branches && st == FZ_SUCCESS; ++i) {
+        fz_workspace* w = nullptr;
+        st              = fz_workspace_create(std::max(max_n, (uint64_t)1), &w);
+        if (st == FZ_SUCCESS) b->own_ws.push_back(w), wss.push_back(w);
     }
+    std::vector<cudaStream_t> cs(branches, nullptr);
+    std::vector<cudaEvent_t>  ev(branches, nullptr);
+    for (uint32_t i = 0; i < branches && st == FZ_SUCCESS; ++i) {
+        if (cudaStreamCreateWithFlags(&cs[i], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) != cudaSuccess)
+            st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
+    }
+    // no timing events inside a graph (event-record nodes would serialise the replay)
+    std::vector<uint32_t> tcap(wss.size());
+    for (size_t i = 0; i < wss.size(); ++i) tcap[i] = wss[i]->tcap, wss[i]->tcap = 0;
     if (st == FZ_SUCCESS) {
-        fz_stream_t h = reinterpret_cast<fz_stream_t>(cs);
-        st = dir == FZ_COMPRESS ? fz_compress_batch(ws, fields, count, eb_mode, mode, h)
-                                : fz_decompress_batch(ws, fields, count, h);
-        cudaGraph_t g = nullptr;
-        e             = cudaStreamEndCapture(cs, &g);
-        if (st == FZ_SUCCESS && e != cudaSuccess) st = map_err(e);
-        b->graph = g;
-        if (st == FZ_SUCCESS) {
-            e = cudaGraphInstantiate(&b->exec, g, 0);
-            if (e != cudaSuccess) st = map_err(e);
+        cudaError_t e = cudaStreamBeginCapture(cs[0], cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) st = map_err(e);
+        else {
+            // fork
+            cudaEventRecord(ev[0], cs[0]);
+            for (uint32_t i = 1; i < branches; ++i) cudaStreamWaitEvent(cs[i], ev[0], 0);
+            for (uint32_t i = 0; i < count && st == FZ_SUCCESS; ++i) {
+                const uint32_t k = i % branches;
+                fz_stream_t    h = reinterpret_cast<fz_stream_t>(cs[k]);
+                st = dir == FZ_COMPRESS ? fz_compress_batch(wss[k], fields + i, 1, eb_mode, mode, h)
+                                        : fz_decompress_batch(wss[k], fields + i, 1, h);
+            }
+            // join
+            for (uint32_t i = 1; i < branches; ++i) {
+                cudaEventRecord(ev[i], cs[i]);
+                cudaStreamWaitEvent(cs[0], ev[i], 0);
+            }
+            cudaGraph_t g = nullptr;
+            e             = cudaStreamEndCapture(cs[0], &g);
+            if (st == FZ_SUCCESS && e != cudaSuccess) st = map_err(e);
+            b->graph = g;
+            if (st == FZ_SUCCESS) {
+                e = cudaGraphInstantiate(&b->exec, g, 0);
+                if (e != cudaSuccess) st = map_err(e);
+            }
         }
     }
-    ws->tcap = tcap;
-    cudaStreamDestroy(cs);
+    for (size_t i = 0; i < wss.size(); ++i) wss[i]->tcap = tcap[i];
+    for (uint32_t i = 0; i < branches; ++i) {
+        if (cs[i]) cudaStreamDestroy(cs[i]);
+        if (ev[i]) cudaEventDestroy(ev[i]);
+    }
     if (st != FZ_SUCCESS) {
         fz_batch_destroy(b);
         return st;
@@ -685,6 +720,7 @@ fz_status fz_batch_destroy(fz_batch* b)
     if (!b) return FZ_INVALID_ARG;
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
+    for (fz_workspace* w : b->own_ws) fz_workspace_destroy(w);
     delete b;
     return FZ_SUCCESS;
 }

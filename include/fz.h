@@ -265,8 +265,11 @@ fz_status fz_decompress_batch(fz_workspace* ws, const fz_field* fields, uint32_t
                               fz_stream_t stream);
 
 /* A batch recorded once into a CUDA graph and replayed with fz_batch_launch; the
-   buffers of `fields` must stay valid while the batch exists.  The scan state's epoch
-   is kept in device memory, so replays with frozen kernel parameters stay correct. */
+   buffers of `fields` must stay valid while the batch exists.  The graph runs the
+   fields on up to 8 parallel branches (round-robin), each with its own workspace (`ws`
+   serves the first; the batch allocates the others), so small fields overlap.  The
+   scan state's epoch is kept in device memory, so replays with frozen kernel
+   parameters stay correct. */
 typedef struct fz_batch fz_batch;
 fz_status fz_batch_create(fz_workspace* ws, const fz_field* fields, uint32_t count,
                           fz_direction dir, fz_eb_mode eb_mode, fz_mode mode, fz_batch** out);
