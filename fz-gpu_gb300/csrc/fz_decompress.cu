@@ -230,21 +230,67 @@ __device__ __forceinline__ void decode_group(const DecodeArgs& a, uint32_t g, ui
     }
 }
 
+// Decoded row buffers (fused 2D/3D paths): a row of the field's window is held as 64-code
+// slots (one decode group each) of eight 16-byte chunks; chunk c of slot G sits at chunk
+// position c ^ (G & 7), so the 16-byte stores of neighbouring groups spread over the banks.
+__device__ __forceinline__ uint32_t rb_chunk(uint32_t G, uint32_t c) { return (G * 8 + (c ^ (G & 7u))) << 2; }
+
+__device__ __forceinline__ void rb_put_group(uint32_t* rb, uint32_t j, const uint32_t (&w)[32])
+{
+#pragma unroll
+    for (uint32_t tt = 0; tt < 8; ++tt)
+        *reinterpret_cast<uint4*>(rb + rb_chunk(j, tt)) = make_uint4(w[4 * tt], w[4 * tt + 1], w[4 * tt + 2], w[4 * tt + 3]);
+}
+
+// Integer deltas of codes i..i+3 of a row buffer.  i % 4 is the same for every thread of
+// a row, so the branch is uniform.
+__device__ __forceinline__ void rb_read4(const uint32_t* rb, uint32_t i, uint32_t (&d)[4])
+{
+    if ((i & 3u) == 0) {
+        const uint2 v = *reinterpret_cast<const uint2*>(rb + rb_chunk(i >> 6, (i >> 3) & 7u) + ((i >> 2) & 1u) * 2);
+        d[0] = sm_decode(v.x & 0xFFFFu), d[1] = sm_decode(v.x >> 16);
+        d[2] = sm_decode(v.y & 0xFFFFu), d[3] = sm_decode(v.y >> 16);
+    } else {
+#pragma unroll
+        for (uint32_t k = 0; k < 4; ++k) {
+            const uint32_t e  = i + k;
+            const uint32_t wv = rb[rb_chunk(e >> 6, (e >> 3) & 7u) + ((e >> 1) & 3u)];
+            d[k]              = sm_decode((e & 1u) ? wv >> 16 : wv & 0xFFFFu);
+        }
+    }
+}
+
+// Stores min(live, 4) reconstructed values at element lin (16-byte store when aligned).
+__device__ __forceinline__ void store4(float* out, uint32_t lin, uint32_t live, const uint32_t (&acc)[4], float ebx2)
+{
+    const float f0 = (float)(int32_t)acc[0] * ebx2, f1 = (float)(int32_t)acc[1] * ebx2;
+    const float f2 = (float)(int32_t)acc[2] * ebx2, f3 = (float)(int32_t)acc[3] * ebx2;
+    if (live >= 4 && (lin & 3u) == 0) {
+        *reinterpret_cast<float4*>(out + lin) = make_float4(f0, f1, f2, f3);
+    } else {
+        out[lin] = f0;
+        if (live > 1) out[lin + 1] = f1;
+        if (live > 2) out[lin + 2] = f2;
+        if (live > 3) out[lin + 3] = f3;
+    }
+}
+
 // ------------------------------------------------------ fused 2D decode --
-// A CTA owns the 16-row tile band blockIdx.y and the 960 columns blockIdx.x (60 tile
-// columns; rows a multiple of 4 elements).  Phase 1: thread (row rr, j) decodes group
-// glo(rr) + j of that row's span into a swizzled row buffer.  Phase 2: thread t owns
-// columns 4t..4t+3; prefix along x (serial + quad shuffles), running sum along y,
-// (float)p * ebx2, coalesced 16-byte stores.  Traffic: the chunks once (plus the at
-// most two groups a row shares with the next window) and the output once.
+// A CTA owns a 16-row tile band and a 960-column window (60 tile columns); the flat
+// block index runs over windows fastest.  Phase 1: thread (row rr, j) decodes group
+// glo(rr) + j of that row's span into the row buffer.  Phase 2: thread t owns columns
+// 4t..4t+3; prefix along x (serial + quad shuffles), running sum along y, (float)p *
+// ebx2, coalesced stores.  Traffic: the chunks once (plus the at most two groups a row
+// shares with the next window) and the output once.
 constexpr uint32_t kW2 = 960;
 
-__global__ void __launch_bounds__(256) k_decompress2d(const DecodeArgs a)
+__global__ void __launch_bounds__(256) k_decompress2d(const DecodeArgs a, uint32_t nwin)
 {
     __shared__ __align__(16) uint32_t rows[16][512];  // 16 rows x 1024 codes
-    const uint32_t tid = threadIdx.x, lane = tid & 31u;
-    const uint32_t c0 = blockIdx.x * kW2, c1 = min(c0 + kW2, a.x);
-    const uint32_t r0 = blockIdx.y * 16;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t bx = blockIdx.x % nwin, by = blockIdx.x / nwin;
+    const uint32_t c0 = bx * kW2, c1 = min(c0 + kW2, a.x);
+    const uint32_t r0 = by * 16;
     {
         const uint32_t rr = tid >> 4, j = tid & 15u, row = r0 + rr;
         if (row < a.y) {
@@ -253,31 +299,21 @@ __global__ void __launch_bounds__(256) k_decompress2d(const DecodeArgs a)
             if (g <= ((lin1 - 1) >> 6)) {
                 uint32_t w[32];
                 decode_group(a, g, w);
-                uint32_t* rb = rows[rr];
-#pragma unroll
-                for (uint32_t tt = 0; tt < 8; ++tt)
-                    *reinterpret_cast<uint4*>(rb + ((j * 8 + (tt ^ (j & 7u))) << 2)) =
-                        make_uint4(w[4 * tt], w[4 * tt + 1], w[4 * tt + 2], w[4 * tt + 3]);
+                rb_put_group(rows[rr], j, w);
             }
         }
     }
     __syncthreads();
-    const uint32_t col = c0 + 4 * tid;
+    const uint32_t col  = c0 + 4 * tid;
     const bool     live = col < c1;
     const uint32_t q    = tid & 3u;
     uint32_t       acc[4] = {0, 0, 0, 0};
     for (uint32_t rr = 0; rr < 16; ++rr) {
         const uint32_t row = r0 + rr;
         if (row >= a.y) break;  // uniform across the CTA
-        uint32_t d[4] = {0, 0, 0, 0};
-        if (live) {
-            const uint32_t lin0 = row * a.x + c0;
-            const uint32_t i    = (lin0 & 63u) + 4 * tid;  // code index in the row buffer
-            const uint32_t G = i >> 6, c = (i >> 3) & 7u;
-            const uint2    v = *reinterpret_cast<const uint2*>(rows[rr] + ((G * 8 + (c ^ (G & 7u))) << 2) + ((i >> 2) & 1u) * 2);
-            d[0] = sm_decode(v.x & 0xFFFFu), d[1] = sm_decode(v.x >> 16);
-            d[2] = sm_decode(v.y & 0xFFFFu), d[3] = sm_decode(v.y >> 16);
-        }
+        const uint32_t lin0 = row * a.x + c0;
+        uint32_t       d[4] = {0, 0, 0, 0};
+        if (live) rb_read4(rows[rr], (lin0 & 63u) + 4 * tid, d);
         d[1] += d[0], d[2] += d[1], d[3] += d[2];
         uint32_t v = d[3];
         uint32_t u = __shfl_up_sync(kFull, v, 1);
@@ -287,13 +323,128 @@ __global__ void __launch_bounds__(256) k_decompress2d(const DecodeArgs a)
         const uint32_t ex = v - d[3];
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[j] += d[j] + ex;
-        if (live)
-            *reinterpret_cast<float4*>(a.out + (size_t)row * a.x + col) =
-                make_float4((float)(int32_t)acc[0] * a.ebx2, (float)(int32_t)acc[1] * a.ebx2,
-                            (float)(int32_t)acc[2] * a.ebx2, (float)(int32_t)acc[3] * a.ebx2);
+        if (live) store4(a.out, lin0 + 4 * tid, c1 - col, acc, a.ebx2);
     }
-    (void)lane;
 }
+
+// ------------------------------------------------------ fused 3D decode --
+// A CTA owns `bands` 8-row tile bands x one 8-plane tile slab x a window of w columns
+// (w a multiple of 8, at most 960); the flat block index runs over windows, then band
+// groups, then slabs.  The slab is walked two planes at a time.  Phase 1 decodes the
+// pass's codes into row buffers: when the window spans whole rows (x <= 960) a plane's
+// rows are one contiguous range of codes, decoded group by group into one buffer of pg
+// slots ("span" mode, no group decoded twice inside the CTA); otherwise each of the
+// bands x 8 rows of a plane gets its own buffer of g slots.  Phase 2: thread (band, cq)
+// owns columns 4cq..4cq+3 of its band; prefix along x within the 8-column tile row (pair
+// shuffle), running sum along y within the plane, running sum along z in zacc, then the
+// stores.
+struct Brick3 {
+    uint32_t w, q2, bands, g;  // window columns, column quads, bands per CTA, slots per row
+    uint32_t nwin, nbgrp;      // windows along x, band groups along y
+    uint32_t span, pg;         // span mode; slots per plane buffer
+};
+constexpr uint32_t kW3 = 960;
+
+__global__ void __launch_bounds__(256, 3) k_decompress3d(const DecodeArgs a, const Brick3 k)
+{
+    extern __shared__ __align__(16) uint32_t rb3[];
+    const uint32_t tid = threadIdx.x;
+    const uint32_t bx = blockIdx.x % k.nwin, rest = blockIdx.x / k.nwin;
+    const uint32_t by = rest % k.nbgrp, bz = rest / k.nbgrp;
+    const uint32_t c0 = bx * k.w, c1 = min(c0 + k.w, a.x);
+    const uint32_t yb0 = by * k.bands, z0 = bz * 8;
+    const uint32_t ys = yb0 * 8, ye = min(ys + 8 * k.bands, a.y);  // the CTA's rows
+    const uint32_t band = tid / k.q2, cq = tid - band * k.q2;
+    const uint32_t col = c0 + 4 * cq, ybase = ys + band * 8;
+    const bool     bandlive = band < k.bands && ybase < a.y;
+    // buffer words per plane (span) or per row
+    const uint32_t rowwords = (k.span ? k.pg : k.g) * 32;
+    const uint32_t ntask    = k.span ? 2 * k.pg : k.bands * 16 * k.g;
+    uint32_t       zacc[8][4];
+#pragma unroll
+    for (int yy = 0; yy < 8; ++yy) zacc[yy][0] = zacc[yy][1] = zacc[yy][2] = zacc[yy][3] = 0;
+    for (uint32_t pz = 0; pz < 8; pz += 2) {
+        if (z0 + pz >= a.z) break;  // uniform across the CTA
+        for (uint32_t task = tid; task < ntask; task += 256) {
+            uint32_t r, j, lin0, lin1;
+            if (k.span) {
+                r = task / k.pg, j = task - r * k.pg;
+                const uint32_t zz = z0 + pz + r;
+                if (zz >= a.z) continue;
+                lin0 = (zz * a.y + ys) * a.x, lin1 = (zz * a.y + ye) * a.x;
+            } else {
+                r = task / k.g, j = task - r * k.g;
+                const uint32_t zz = z0 + pz + ((r >> 3) & 1u), yv = ys + (r >> 4) * 8 + (r & 7u);
+                if (zz >= a.z || yv >= a.y) continue;
+                lin0 = (zz * a.y + yv) * a.x + c0, lin1 = lin0 + (c1 - c0);
+            }
+            const uint32_t g = (lin0 >> 6) + j;
+            if (g > ((lin1 - 1) >> 6)) continue;
+            uint32_t w[32];
+            decode_group(a, g, w);
+            rb_put_group(rb3 + r * rowwords, j, w);
+        }
+        __syncthreads();
+        for (uint32_t p = 0; p < 2; ++p) {
+            const uint32_t zz = z0 + pz + p;
+            if (zz >= a.z) break;  // uniform across the CTA
+            const uint32_t pbase = ((zz * a.y + ys) * a.x) & ~63u;  // span mode: first slot's code
+            uint32_t       colacc[4] = {0, 0, 0, 0};
+#pragma unroll
+            for (uint32_t yy = 0; yy < 8; ++yy) {
+                const uint32_t yv   = ybase + yy;
+                const bool     live = bandlive && yv < a.y && col < c1;
+                const uint32_t lin0 = (zz * a.y + yv) * a.x + c0;
+                uint32_t       d[4] = {0, 0, 0, 0};
+                if (live) {
+                    if (k.span) rb_read4(rb3 + p * rowwords, lin0 + 4 * cq - pbase, d);
+                    else rb_read4(rb3 + (band * 16 + p * 8 + yy) * rowwords, (lin0 & 63u) + 4 * cq, d);
+                }
+                d[1] += d[0], d[2] += d[1], d[3] += d[2];
+                const uint32_t u  = __shfl_up_sync(kFull, d[3], 1);
+                const uint32_t ex = (cq & 1u) ? u : 0u;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    colacc[j] += d[j] + ex;
+                    zacc[yy][j] += colacc[j];
+                }
+                if (live) store4(a.out, lin0 + 4 * cq, c1 - col, zacc[yy], a.ebx2);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Brick shape of the fused 3D path for a field of width x and height y.  Span mode
+// (whole rows) takes as many bands as keep both the compute threads (bands x q2) and the
+// pass's decode tasks (2 pg) within the CTA's 256 threads.
+static Brick3 brick3(uint32_t x, uint32_t y)
+{
+    Brick3 k{};
+    k.w  = std::min<uint32_t>(kW3, (x + 7) & ~7u);
+    k.q2 = k.w / 4;
+    k.g  = (k.w + 62) / 64 + 1;
+    k.nwin = (uint32_t)cdiv(x, k.w);
+    const uint32_t nbands = (uint32_t)cdiv(y, 8);
+    k.span = k.nwin == 1;
+    if (k.span) {
+        k.bands = std::max(1u, std::min(256u / k.q2, nbands));
+        for (;;) {
+            // a plane's span is at most 8 bands x rows of x codes, starting anywhere in a group;
+            // rows' last quads read up to 3 codes past it
+            k.pg = (8 * k.bands * x + 66) / 64 + 1;
+            if (k.bands == 1 || 2 * k.pg <= 256) break;
+            --k.bands;
+        }
+    } else {
+        k.bands = std::max(1u, std::min({8u, 256u / k.q2, nbands}));
+        while (k.bands > 1 && k.bands * 16 * k.g * 128 > 48 * 1024) --k.bands;
+    }
+    k.nbgrp = (uint32_t)cdiv(nbands, k.bands);
+    return k;
+}
+
+static uint32_t brick3_smem(const Brick3& k) { return k.span ? 2 * k.pg * 128 : k.bands * 16 * k.g * 128; }
 
 // ------------------------------------------------------ fused 1D decode --
 // One warp per shuffle block: lane g decodes its 64 codes (a quarter of one 256-element
@@ -370,28 +521,31 @@ __global__ void __launch_bounds__(kDecode1dWarps * 32) k_decompress1d(const Deco
 cudaError_t launch_decompress_fused(const DecodeArgs& a, cudaStream_t s)
 {
     const int nd = (a.z == 1 && a.y == 1) ? 1 : (a.z == 1 ? 2 : 3);
-    if (nd == 2 && a.x % 4 == 0) {
-        dim3 grid((uint32_t)cdiv(a.x, kW2), (uint32_t)cdiv(a.y, 16));
-        k_decompress2d<<<grid, 256, 0, s>>>(a);
+    if (nd == 2) {
+        const uint32_t nwin = (uint32_t)cdiv(a.x, kW2);
+        k_decompress2d<<<(uint32_t)(nwin * cdiv(a.y, 16)), 256, 0, s>>>(a, nwin);
         return cudaGetLastError();
     }
-    if (nd == 1) {
-        const uint32_t ntiles = a.nb + (a.tail ? 1u : 0u);
-        k_decompress1d<<<(uint32_t)cdiv(ntiles, kDecode1dWarps), kDecode1dWarps * 32, 0, s>>>(a);
+    if (nd == 3) {
+        const Brick3   k    = brick3(a.x, a.y);
+        const uint64_t ctas = (uint64_t)k.nwin * k.nbgrp * cdiv(a.z, 8);
+        k_decompress3d<<<(uint32_t)ctas, 256, brick3_smem(k), s>>>(a, k);
         return cudaGetLastError();
     }
-    return cudaErrorNotSupported;
+    const uint32_t ntiles = a.nb + (a.tail ? 1u : 0u);
+    k_decompress1d<<<(uint32_t)cdiv(ntiles, kDecode1dWarps), kDecode1dWarps * 32, 0, s>>>(a);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------- recon --
 // 2D: a CTA covers 16 rows x 512 columns; lane owns 4 consecutive columns, lanes 4k..4k+3
 // one 16-column tile row.  Row prefix: serial over 4 + quad shuffle scan; column prefix:
 // running sum over the 16 rows.
-__global__ void __launch_bounds__(128) k_recon2d(const ReconArgs a)
+__global__ void __launch_bounds__(128) k_recon2d(const ReconArgs a, uint32_t nwin)
 {
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-    const uint32_t c0   = blockIdx.x * 512 + wid * 128 + lane * 4;
-    const uint32_t r0   = blockIdx.y * 16;
+    const uint32_t c0   = (blockIdx.x % nwin) * 512 + wid * 128 + lane * 4;
+    const uint32_t r0   = (blockIdx.x / nwin) * 16;
     const uint32_t q    = lane & 3u;
     const bool     vec  = (a.x % 4 == 0) && (c0 + 3 < a.x);
     uint32_t       acc[4] = {0, 0, 0, 0};
@@ -432,12 +586,14 @@ __global__ void __launch_bounds__(128) k_recon2d(const ReconArgs a)
 
 // 3D: a warp covers 128 columns of one 8x8 (y, z) tile column; lane owns 4 columns, lane
 // pairs one 8-column tile row.  zacc[y] keeps the running z-sum of each of the 8 rows.
-__global__ void __launch_bounds__(128) k_recon3d(const ReconArgs a)
+// The flat block index runs over x windows, then groups of 4 bands, then z slabs.
+__global__ void __launch_bounds__(128) k_recon3d(const ReconArgs a, uint32_t nwin, uint32_t nyg)
 {
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-    const uint32_t c0   = blockIdx.x * 128 + lane * 4;
-    const uint32_t y0   = (blockIdx.y * 4 + wid) * 8;
-    const uint32_t z0   = blockIdx.z * 8;
+    const uint32_t rest = blockIdx.x / nwin;
+    const uint32_t c0   = (blockIdx.x % nwin) * 128 + lane * 4;
+    const uint32_t y0   = ((rest % nyg) * 4 + wid) * 8;
+    const uint32_t z0   = (rest / nyg) * 8;
     if (y0 >= a.y) return;  // warp-uniform
     const bool     vec = (a.x % 4 == 0) && (c0 + 3 < a.x);
     const size_t   xy  = (size_t)a.x * a.y;
@@ -559,11 +715,11 @@ cudaError_t launch_reconstruct(const ReconArgs& a, cudaStream_t s)
     if (nd == 1) {
         k_recon1d<<<(uint32_t)cdiv(cdiv(a.nl, 256), 8), 256, 0, s>>>(a);
     } else if (nd == 2) {
-        dim3 grid((uint32_t)cdiv(a.x, 512), (uint32_t)cdiv(a.y, 16));
-        k_recon2d<<<grid, 128, 0, s>>>(a);
+        const uint32_t nwin = (uint32_t)cdiv(a.x, 512);
+        k_recon2d<<<(uint32_t)(nwin * cdiv(a.y, 16)), 128, 0, s>>>(a, nwin);
     } else {
-        dim3 grid((uint32_t)cdiv(a.x, 128), (uint32_t)cdiv(cdiv(a.y, 8), 4), (uint32_t)cdiv(a.z, 8));
-        k_recon3d<<<grid, 128, 0, s>>>(a);
+        const uint32_t nwin = (uint32_t)cdiv(a.x, 128), nyg = (uint32_t)cdiv(cdiv(a.y, 8), 4);
+        k_recon3d<<<(uint32_t)((uint64_t)nwin * nyg * cdiv(a.z, 8)), 128, 0, s>>>(a, nwin, nyg);
     }
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && a.n > a.nl) {

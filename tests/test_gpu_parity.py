@@ -38,6 +38,7 @@ SMALL = [
     ("smooth2d", (300, 70, 1), 1e-3), ("peaks2d", (400, 90, 1), 1e-4), ("smooth2d", (101, 37, 1), 1e-3),
     ("smooth2d", (1, 3000, 1), 1e-3), ("smooth2d", (17, 2049, 1), 1e-2), ("smooth3d", (40, 33, 20), 1e-3),
     ("smooth3d", (37, 19, 11), 1e-2), ("smooth3d", (33, 1, 70), 1e-3), ("smooth3d", (9, 9, 9), 1e-3),
+    ("smooth3d", (7, 300, 2), 1e-3), ("smooth3d", (63, 130, 3), 1e-3), ("smooth3d", (961, 20, 9), 1e-3),
     ("smooth1d", (100000, 1, 1), 1e-3), ("smooth1d", (1500, 1, 1), 1e-3), ("smooth1d", (2048, 1, 1), 1e-3),
     ("smooth1d", (4097, 1, 1), 1e-4), ("smooth2d", (64, 32, 1), 1e-3), ("smooth1d", (7, 1, 1), 1e-3),
 ]
@@ -55,6 +56,29 @@ def test_compress_decompress_small(fz, oracle, synth, ws, kind, dims, eb, mode):
     if mode == 1:
         h = oracle.parse_header(want)
         assert (np.abs(rec.astype(np.float64) - data) <= error_tolerance(data, h["eb_abs"])).all()
+
+
+TALL = [((4, 1 << 21, 1), 1e-3), ((6, 1 << 20, 1), 1e-3), ((8, 1 << 21, 2), 1e-3), ((5, 1 << 19, 3), 1e-2)]
+
+
+@pytest.mark.parametrize("dims,eb", TALL, ids=["x".join(map(str, d)) for d, _ in TALL])
+def test_tall_fields(fz, oracle, ws, dims, eb):
+    """Fields with more than 65535 tile bands along y: the decompression kernels index
+    their CTAs with a flat block index, so these launch and match the oracle."""
+    n = dims[0] * dims[1] * dims[2]
+    rng = np.random.default_rng(n)
+    data = np.cumsum(rng.normal(0, 1, n)).astype(np.float32)
+    st, got, want = run_both(fz, oracle, ws, data, dims, eb, mode=1)
+    assert_same_stream(got, want)
+    rec = fz.decompress(st, ws=ws).cpu().numpy()
+    assert np.array_equal(rec.view(np.uint32), oracle.decompress(want).view(np.uint32))
+    # the two-pass reconstruction kernels behind the stage API
+    eb_abs = oracle.parse_header(want)["eb_abs"]
+    codes, _, _ = oracle.lorenzo_construct(data, dims, oracle.ebx2_r(eb_abs))
+    q = torch.from_numpy(codes.view(np.int16)).cuda()
+    rec2 = fz.lorenzo_reconstruct(q, dims, eb_abs).cpu().numpy()
+    rec2_o = oracle.lorenzo_reconstruct(codes, dims, oracle.ebx2(eb_abs))
+    assert np.array_equal(rec2.view(np.uint32), rec2_o.view(np.uint32))
 
 
 FULL = [
