@@ -187,6 +187,98 @@ __device__ __forceinline__ void block2d(const float* __restrict__ in, const Geo&
     ovf |= ov ? 1u : 0u;
 }
 
+// Plane/row/column of element e0 + 128 given that of e0 (x a multiple of 4).
+__device__ __forceinline__ void advance128_3d(const Geo& g, uint32_t e0, uint32_t& zz, uint32_t& yy,
+                                              uint32_t& xx)
+{
+    if (g.x >= 128) {
+        xx += 128;
+        if (xx >= g.x) {
+            xx -= g.x;
+            if (++yy == g.y) yy = 0, ++zz;
+        }
+    } else {
+        const uint32_t e = e0 + 128;
+        zz               = fdiv(e, g.dxy);
+        const uint32_t rem = e - zz * g.xy;
+        yy               = fdiv(rem, g.dx), xx = rem - yy * g.x;
+    }
+}
+
+// A whole 3D shuffle block [base, base+2048) inside x*y*z with rows a multiple of 4
+// elements long (so a lane's 4 elements share one row, and the halo rows -- north,
+// below, below-north -- are 16-byte aligned).  Same float expressions as fast3d; the
+// west neighbours of lane 0 (prequantised c, n, b, bn of element e0-1) are carried from
+// lane 31 of the previous group row, coordinates advance incrementally, and the loads of
+// group row it+1 are issued before group row it is processed.
+__device__ __forceinline__ void block3d(const float* __restrict__ in, const Geo& g, uint32_t base, float r,
+                                        uint32_t lane, uint32_t* sm, uint32_t& ovf)
+{
+    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint32_t     e0 = base + lane * 4;
+    uint32_t     zz = fdiv(e0, g.dxy);
+    uint32_t     yy = fdiv(e0 - zz * g.xy, g.dx), xx = e0 - zz * g.xy - yy * g.x;
+    bool         zi = (zz & 7u) != 0, yi = (yy & 7u) != 0;
+    float4       v = ldg4(in + e0);
+    float4       un = yi ? ldg4(in + (e0 - g.x)) : z4;
+    float4       ub = zi ? ldg4(in + (e0 - g.xy)) : z4;
+    float4       uc = (zi && yi) ? ldg4(in + (e0 - g.xy - g.x)) : z4;
+    // prequantised c, n, b, bn of element base-1 (lane 0's west neighbour)
+    float cw = 0.0f, nw = 0.0f, bw = 0.0f, bnw = 0.0f;
+    if (lane == 0 && (xx & 7u)) {
+        cw  = pq(__ldg(in + e0 - 1), r);
+        nw  = yi ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f;
+        bw  = zi ? pq(__ldg(in + e0 - 1 - g.xy), r) : 0.0f;
+        bnw = (zi && yi) ? pq(__ldg(in + e0 - 1 - g.xy - g.x), r) : 0.0f;
+    }
+    bool ov = false;
+#pragma unroll 1
+    for (uint32_t it = 0; it < 16; ++it) {
+        uint32_t zn = zz, yn = yy, xn = xx;
+        float4   vn = z4, unn = z4, ubn = z4, ucn = z4;
+        if (it < 15) {
+            advance128_3d(g, e0, zn, yn, xn);
+            const bool zin = (zn & 7u) != 0, yin = (yn & 7u) != 0;
+            const uint32_t e1 = e0 + 128;
+            vn = ldg4(in + e1);
+            if (yin) unn = ldg4(in + (e1 - g.x));
+            if (zin) ubn = ldg4(in + (e1 - g.xy));
+            if (zin && yin) ucn = ldg4(in + (e1 - g.xy - g.x));
+        }
+        const float p[4]  = {pq(v.x, r), pq(v.y, r), pq(v.z, r), pq(v.w, r)};
+        const float nq[4] = {pq(un.x, r), pq(un.y, r), pq(un.z, r), pq(un.w, r)};
+        const float bq[4] = {pq(ub.x, r), pq(ub.y, r), pq(ub.z, r), pq(ub.w, r)};
+        const float bn[4] = {pq(uc.x, r), pq(uc.y, r), pq(uc.z, r), pq(uc.w, r)};
+        float       wp = __shfl_up_sync(kFull, p[3], 1), wn = __shfl_up_sync(kFull, nq[3], 1);
+        float       wb = __shfl_up_sync(kFull, bq[3], 1), wbn = __shfl_up_sync(kFull, bn[3], 1);
+        if (lane == 0) wp = cw, wn = nw, wb = bw, wbn = bnw;
+        cw  = __shfl_sync(kFull, p[3], 31);
+        nw  = __shfl_sync(kFull, nq[3], 31);
+        bw  = __shfl_sync(kFull, bq[3], 31);
+        bnw = __shfl_sync(kFull, bn[3], 31);
+        if ((xx & 7u) == 0) wp = wn = wb = wbn = 0.0f;  // the group starts a tile row
+        uint32_t c[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            // c - (A - B - C - D + E + F + G), lorenzo_var.cuh:277-283; absent terms are 0
+            float s = __fsub_rn(j ? bn[j - 1] : wbn, j ? nq[j - 1] : wn);
+            s       = __fsub_rn(s, j ? bq[j - 1] : wb);
+            s       = __fsub_rn(s, bn[j]);
+            s       = __fadd_rn(s, j ? p[j - 1] : wp);
+            s       = __fadd_rn(s, nq[j]);
+            s       = __fadd_rn(s, bq[j]);
+            const float d = __fsub_rn(p[j], s);
+            c[j]          = pack_signed(d);
+            ov |= !(fabsf(d) < 32768.0f);
+        }
+        const uint32_t q = it * 16 + (lane >> 1);
+        *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+        v = vn, un = unn, ub = ubn, uc = ucn, zz = zn, yy = yn, xx = xn;
+        e0 += 128;
+    }
+    ovf |= ov ? 1u : 0u;
+}
+
 template <int ND>
 __device__ __forceinline__ void codes4(const float* __restrict__ in, const Geo& g, uint32_t e0,
                                        float r, uint32_t lane, uint32_t (&code)[4],
@@ -391,173 +483,197 @@ __device__ void write_header(const CompressArgs& a, const EbInfo& e, uint32_t ov
 }
 
 
+// Phases A-C for shuffle block t of the field: its codes into the warp's shared buffer
+// `sm` (swizzled), the bit transpose, the shuffled image back into `sm`, the chunk flags
+// as 8 ballots (= bitmap words 8t..8t+7, stored), the chunk count and the overflow bit.
+// Block t == nb (the n mod 2048 tail, never shuffled, fz.cu:173) writes its codes to the
+// sidecar and zero-fills the 16-byte pads of Sections A and C.
+template <int ND>
+__device__ __forceinline__ void compute_block(const CompressArgs& a, const Geo& g, uint32_t t, float r,
+                                              uint32_t lane, uint32_t* sm, uint32_t* signw,
+                                              uint32_t (&bm)[8], uint32_t& cnt, uint32_t& ovf)
+{
+    const uint32_t base = t * kBlockCodes;
+    if (t < a.nb) {
+        // ---- phase A: codes of the block into shared memory (swizzled) ----
+        if (ND == 2 && g.al_x && base + kBlockCodes <= g.nl) {
+            block2d(a.in, g, base, r, lane, sm, ovf);
+        } else if (ND == 3 && g.al_x && base + kBlockCodes <= g.nl) {
+            block3d(a.in, g, base, r, lane, sm, ovf);
+        } else {
+#pragma unroll 4
+            for (uint32_t it = 0; it < 16u; ++it) {
+                const uint32_t e0 = base + it * 128 + lane * 4;
+                uint32_t       c[4], sgn = 0;
+                codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
+                const uint32_t q = it * 16 + (lane >> 1);
+                *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
+                    make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+                if (ND == 1 && signw) {
+                    // 4 sign bits per lane -> one u32 per 8 lanes (32 consecutive elements)
+                    uint32_t v = sgn << ((lane & 7u) * 4);
+                    v |= __shfl_xor_sync(kFull, v, 1);
+                    v |= __shfl_xor_sync(kFull, v, 2);
+                    v |= __shfl_xor_sync(kFull, v, 4);
+                    if ((lane & 7u) == 0) signw[(base >> 5) + it * 4 + (lane >> 3)] = v;
+                }
+            }
+        }
+        __syncwarp();
+        // ---- phase B: lane g transposes group g (words g*32 .. g*32+31) ----
+        uint32_t w[32];
+#pragma unroll
+        for (uint32_t tt = 0; tt < 8; ++tt) {
+            const uint4 v = *reinterpret_cast<const uint4*>(sm + swz(lane * 8 + tt));
+            w[4 * tt] = v.x, w[4 * tt + 1] = v.y, w[4 * tt + 2] = v.z, w[4 * tt + 3] = v.w;
+        }
+        transpose32(w);
+        __syncwarp();
+        // shuffled image S[p*32 + g] = w[p] (bitshuffleAndBitflag's out, fz.cu:82)
+#pragma unroll
+        for (uint32_t p = 0; p < 32; ++p) sm[p * 32 + lane] = w[p];
+        __syncwarp();
+        // ---- phase C: chunk c = lane + 32 i; ballot i is bitmap word 8t+i ----
+#pragma unroll
+        for (uint32_t i = 0; i < 8; ++i) {
+            const uint4 v = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
+            bm[i] = __ballot_sync(kFull, (v.x | v.y | v.z | v.w) != 0);
+            cnt += __popc(bm[i]);
+        }
+        if (lane == 0) {
+            uint4* A = reinterpret_cast<uint4*>(a.out + a.off_a) + 2 * (size_t)t;
+            A[0]     = make_uint4(bm[0], bm[1], bm[2], bm[3]);
+            A[1]     = make_uint4(bm[4], bm[5], bm[6], bm[7]);
+        }
+    } else if (t == a.nb && a.n > base) {
+        // ---- tail block: n mod 2048 codes, never shuffled (fz.cu:173) ----
+        const uint32_t tail = a.n - base;
+        uint16_t*      tc   = (a.mode == 1) ? reinterpret_cast<uint16_t*>(a.out + a.off_c) : nullptr;
+        for (uint32_t it = 0; it * 128 < tail; ++it) {
+            const uint32_t e0 = base + it * 128 + lane * 4;
+            uint32_t       c[4], sgn = 0;
+            codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (tc && e0 + j < a.n) tc[e0 + j - base] = (uint16_t)c[j];
+            if (ND == 1 && signw) {
+                uint32_t v = sgn << ((lane & 7u) * 4);
+                v |= __shfl_xor_sync(kFull, v, 1);
+                v |= __shfl_xor_sync(kFull, v, 2);
+                v |= __shfl_xor_sync(kFull, v, 4);
+                const uint32_t wi = (base >> 5) + it * 4 + (lane >> 3);
+                if ((lane & 7u) == 0 && wi * 32 < a.n) signw[wi] = v;
+            }
+        }
+        // zero padding of the tail code array and of the sign array
+        if (tc)
+            for (uint32_t i = tail + lane; i < (uint32_t)(pad16(2 * (uint64_t)tail) / 2); i += 32) tc[i] = 0;
+        if (ND == 1 && signw) {
+            const uint32_t nsw = (uint32_t)cdiv(a.n, 32);
+            const uint32_t pw  = (uint32_t)(pad16(4 * (uint64_t)nsw) / 4);
+            for (uint32_t i = nsw + lane; i < pw; i += 32) signw[i] = 0;
+        }
+        // bitmap words of the partial block are zero (fz.cu:167), then the 16-byte pad
+        uint32_t*      A  = reinterpret_cast<uint32_t*>(a.out + a.off_a);
+        const uint32_t pa = (uint32_t)(pad16(4 * (uint64_t)a.nwords) / 4);
+        for (uint32_t i = a.nb * 8 + lane; i < pa; i += 32) A[i] = 0;
+    }
+    ovf = __reduce_or_sync(kFull, ovf);
+}
+
 // Persistent: one resident wave of CTAs; each CTA repeatedly takes the next scan tile
 // (8 shuffle blocks, one per warp) from the ticket counter.  Tickets are handed out in
 // order, so every predecessor of a tile has been taken by a running CTA and the
-// look-back always makes progress.  The last of the nct + gridDim.x fetches resets the
-// counter, the range accumulators and advances the epoch.
+// look-back always makes progress, whatever else runs on the GPU.  The last of the
+// nct + gridDim.x fetches resets the counter, the range accumulators and advances the
+// epoch.
 //
-// Software pipeline over a CTA's tiles, shared memory double-buffered: iteration k
-// computes tile k (codes, transposes, flags, aggregate published), then resolves tile
-// k-1 (look-back, offsets, compacted stores).  By then tile k-1's predecessors have long
-// published their inclusive prefixes, so its look-back is about one round trip instead
-// of a walk past every tile in flight.
+// Software pipeline over a CTA's tiles, shared memory double-buffered, two CTA barriers
+// per tile: iteration k computes tile k (codes, transposes, flags) -- thread 0 takes the
+// CTA's next ticket as soon as its own block is done -- then warp 0 publishes tile k's
+// aggregate and resolves tile k-1 (look-back, inclusive prefix, per-block offsets), and
+// every warp writes its block of tile k-1.  By then tile k-1's predecessors have long
+// published, so its look-back is about one round trip.
 template <int ND>
 __global__ void __launch_bounds__(kCompressWarps * 32, 3) k_compress(const CompressArgs a)
 {
     extern __shared__ __align__(16) uint32_t dsm[];  // [2][kCompressWarps][kBlockWords]
     __shared__ uint32_t s_cnt[2][kCompressWarps], s_ovf[2][kCompressWarps], s_tile[2], s_tot[2];
-    __shared__ uint32_t s_excl, s_epoch;
+    __shared__ uint32_t s_pre[kCompressWarps], s_epoch;
     __shared__ EbInfo   s_eb;
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     const uint32_t nct  = (uint32_t)cdiv(a.ntiles, kCompressWarps);
+    const uint32_t nfetch = nct + gridDim.x;
 
     if (threadIdx.x == 0) {
         s_eb    = a.mm ? eb_from_range(ord2f(__ldcg(a.mm)), ord2f(__ldcg(a.mm + 1)), a.eb_rel) : a.ebh;
         s_epoch = __ldcg(a.epoch);
         __threadfence();  // both reads complete before the first ticket (the last one resets them)
+        const Ticket tk = take_ticket(a.ticket, a.epoch, nfetch);
+        if (tk.last && a.mm) a.mm[0] = 0xFFFFFFFFu, a.mm[1] = 0u;  // empty range for the next call
+        s_tile[0] = tk.tile;
     }
+    __syncthreads();
+    const EbInfo   eb    = s_eb;
+    const uint32_t epoch = s_epoch;
     Geo g;
     g.nl = a.nl, g.x = a.x, g.y = a.y, g.xy = a.xy, g.lim = a.n;
     g.dx = a.dx, g.dxy = a.dxy, g.al_x = a.al_x, g.al_xy = a.al_xy, g.al_xyx = a.al_xyx;
     uint32_t* signw = (ND == 1 && a.mode == 1) ? reinterpret_cast<uint32_t*>(a.out + a.off_sign) : nullptr;
     uint32_t  bm_prev[8];  // bitmap words of this warp's block of the previous tile
+    uint32_t  prev_ct = 0;
 
     for (uint32_t k = 0;; ++k) {
-        const uint32_t buf = k & 1u;
-        uint32_t*      sm  = dsm + (buf * kCompressWarps + wid) * kBlockWords;
-        if (threadIdx.x == 0) {
-            const Ticket tk = take_ticket(a.ticket, a.epoch, nct + gridDim.x);
-            if (tk.last && a.mm) a.mm[0] = 0xFFFFFFFFu, a.mm[1] = 0u;  // empty range for the next call
-            s_tile[buf] = tk.tile;
-        }
-        __syncthreads();
+        const uint32_t buf   = k & 1u;
+        uint32_t*      sm    = dsm + (buf * kCompressWarps + wid) * kBlockWords;
         const uint32_t ct    = s_tile[buf];
         const bool     have  = ct < nct;  // uniform
-        const EbInfo   eb    = s_eb;
-        const uint32_t epoch = s_epoch;
         uint32_t       bm[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
         if (have) {
-            const float    r    = eb.ebx2_r;
-            const uint32_t t    = ct * kCompressWarps + wid;  // this warp's shuffle block
-            const uint32_t base = t * kBlockCodes;
-            uint32_t       ovf  = 0, cnt = 0;
-            if (ND == 2 && t < a.nb && g.al_x && base + kBlockCodes <= g.nl) {
-                block2d(a.in, g, base, r, lane, sm, ovf);
-            }
-            if (t < a.nb) {
-                // ---- phase A: codes of the block into shared memory (swizzled) ----
-#pragma unroll 4
-                for (uint32_t it = 0; it < ((ND == 2 && g.al_x && base + kBlockCodes <= g.nl) ? 0u : 16u); ++it) {
-                    const uint32_t e0 = base + it * 128 + lane * 4;
-                    uint32_t       c[4], sgn = 0;
-                    codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
-                    const uint32_t q = it * 16 + (lane >> 1);
-                    *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
-                        make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
-                    if (ND == 1 && signw) {
-                        // 4 sign bits per lane -> one u32 per 8 lanes (32 consecutive elements)
-                        uint32_t v = sgn << ((lane & 7u) * 4);
-                        v |= __shfl_xor_sync(kFull, v, 1);
-                        v |= __shfl_xor_sync(kFull, v, 2);
-                        v |= __shfl_xor_sync(kFull, v, 4);
-                        if ((lane & 7u) == 0) signw[(base >> 5) + it * 4 + (lane >> 3)] = v;
-                    }
-                }
-                __syncwarp();
-                // ---- phase B: lane g transposes group g (words g*32 .. g*32+31) ----
-                uint32_t w[32];
-#pragma unroll
-                for (uint32_t tt = 0; tt < 8; ++tt) {
-                    const uint4 v = *reinterpret_cast<const uint4*>(sm + swz(lane * 8 + tt));
-                    w[4 * tt] = v.x, w[4 * tt + 1] = v.y, w[4 * tt + 2] = v.z, w[4 * tt + 3] = v.w;
-                }
-                transpose32(w);
-                __syncwarp();
-                // shuffled image S[p*32 + g] = w[p] (bitshuffleAndBitflag's out, fz.cu:82)
-#pragma unroll
-                for (uint32_t p = 0; p < 32; ++p) sm[p * 32 + lane] = w[p];
-                __syncwarp();
-                // ---- phase C: chunk c = lane + 32 i; ballot i is bitmap word 8t+i ----
-#pragma unroll
-                for (uint32_t i = 0; i < 8; ++i) {
-                    const uint4 v = *reinterpret_cast<const uint4*>(sm + (lane + 32 * i) * 4);
-                    bm[i] = __ballot_sync(kFull, (v.x | v.y | v.z | v.w) != 0);
-                    cnt += __popc(bm[i]);
-                }
-                if (lane == 0) {
-                    uint4* A = reinterpret_cast<uint4*>(a.out + a.off_a) + 2 * (size_t)t;
-                    A[0]     = make_uint4(bm[0], bm[1], bm[2], bm[3]);
-                    A[1]     = make_uint4(bm[4], bm[5], bm[6], bm[7]);
-                }
-            } else if (t == a.nb && a.n > base) {
-                // ---- tail block: n mod 2048 codes, never shuffled (fz.cu:173) ----
-                const uint32_t tail = a.n - base;
-                uint16_t*      tc   = (a.mode == 1) ? reinterpret_cast<uint16_t*>(a.out + a.off_c) : nullptr;
-                for (uint32_t it = 0; it * 128 < tail; ++it) {
-                    const uint32_t e0 = base + it * 128 + lane * 4;
-                    uint32_t       c[4], sgn = 0;
-                    codes4<ND>(a.in, g, e0, r, lane, c, ovf, sgn);
-#pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        if (tc && e0 + j < a.n) tc[e0 + j - base] = (uint16_t)c[j];
-                    if (ND == 1 && signw) {
-                        uint32_t v = sgn << ((lane & 7u) * 4);
-                        v |= __shfl_xor_sync(kFull, v, 1);
-                        v |= __shfl_xor_sync(kFull, v, 2);
-                        v |= __shfl_xor_sync(kFull, v, 4);
-                        const uint32_t wi = (base >> 5) + it * 4 + (lane >> 3);
-                        if ((lane & 7u) == 0 && wi * 32 < a.n) signw[wi] = v;
-                    }
-                }
-                // zero padding of the tail code array and of the sign array
-                if (tc)
-                    for (uint32_t i = tail + lane; i < (uint32_t)(pad16(2 * (uint64_t)tail) / 2); i += 32) tc[i] = 0;
-                if (ND == 1 && signw) {
-                    const uint32_t nsw = (uint32_t)cdiv(a.n, 32);
-                    const uint32_t pw  = (uint32_t)(pad16(4 * (uint64_t)nsw) / 4);
-                    for (uint32_t i = nsw + lane; i < pw; i += 32) signw[i] = 0;
-                }
-                // bitmap words of the partial block are zero (fz.cu:167), then the 16-byte pad
-                uint32_t*      A  = reinterpret_cast<uint32_t*>(a.out + a.off_a);
-                const uint32_t pa = (uint32_t)(pad16(4 * (uint64_t)a.nwords) / 4);
-                for (uint32_t i = a.nb * 8 + lane; i < pa; i += 32) A[i] = 0;
-            }
-            ovf = __reduce_or_sync(kFull, ovf);
+            uint32_t ovf = 0, cnt = 0;
+            compute_block<ND>(a, g, ct * kCompressWarps + wid, eb.ebx2_r, lane, sm, signw, bm, cnt, ovf);
             if (lane == 0) s_cnt[buf][wid] = cnt, s_ovf[buf][wid] = ovf;
+            if (threadIdx.x == 0) {  // the CTA's next tile; slot buf^1 (tile k-1) is read only via prev_ct now
+                const Ticket tk = take_ticket(a.ticket, a.epoch, nfetch);
+                if (tk.last && a.mm) a.mm[0] = 0xFFFFFFFFu, a.mm[1] = 0u;
+                s_tile[buf ^ 1u] = tk.tile;
+            }
         }
         __syncthreads();
-        // ---- tile k: CTA aggregate published; tile k-1: look-back and offset ----
+        // ---- tile k: CTA aggregate published; tile k-1: look-back and block offsets ----
         if (wid == 0) {
             if (have) {
                 const uint32_t tot = __reduce_add_sync(kFull, lane < kCompressWarps ? s_cnt[buf][lane] : 0u);
                 const uint32_t tov = __reduce_or_sync(kFull, lane < kCompressWarps ? s_ovf[buf][lane] : 0u);
                 if (lane == 0) {
                     s_tot[buf] = tot;
-                    if (ct == 0) publish(a.state, 0, epoch, kFlagIncl, tov, tot);
-                    else publish(a.state, ct, epoch, kFlagAgg, tov, tot);
+                    publish(a.state, ct, epoch, ct == 0 ? kFlagIncl : kFlagAgg, tov, tot);
                 }
             }
             if (k > 0) {
-                const uint32_t pb  = buf ^ 1u;
-                const uint32_t pct = s_tile[pb];
-                const uint32_t tot = s_tot[pb];
-                const uint32_t tov = __reduce_or_sync(kFull, lane < kCompressWarps ? s_ovf[pb][lane] : 0u);
+                const uint32_t pb   = buf ^ 1u;
+                const uint32_t tot  = s_tot[pb];
+                const uint32_t c    = lane < kCompressWarps ? s_cnt[pb][lane] : 0u;
+                const uint32_t tov  = __reduce_or_sync(kFull, lane < kCompressWarps ? s_ovf[pb][lane] : 0u);
                 uint32_t       excl = 0, povf = 0;
-                if (pct != 0) {
-                    lookback(a.state, pct, epoch, a.status, excl, povf);
-                    if (lane == 0) publish(a.state, pct, epoch, kFlagIncl, tov | povf, excl + tot);
+                if (prev_ct != 0) {
+                    lookback(a.state, prev_ct, epoch, a.status, excl, povf);
+                    if (lane == 0) publish(a.state, prev_ct, epoch, kFlagIncl, tov | povf, excl + tot);
                 }
-                if (lane == 0) {
-                    s_excl = excl;
-                    if (pct == nct - 1) {
-                        write_header(a, eb, tov | povf, excl + tot);
-                        if (a.boff) {
-                            // the total closes the offset table; zero its 16-byte pad
-                            a.boff[a.nb] = excl + tot;
-                            for (uint32_t i = a.nb + 1; i < (uint32_t)(pad16(4ull * (a.nb + 1)) / 4); ++i) a.boff[i] = 0;
-                        }
+                uint32_t inc = c;  // exclusive offsets of tile k-1's blocks
+#pragma unroll
+                for (uint32_t o = 1; o < kCompressWarps; o <<= 1) {
+                    const uint32_t v = __shfl_up_sync(kFull, inc, o);
+                    if (lane >= o) inc += v;
+                }
+                if (lane < kCompressWarps) s_pre[lane] = excl + inc - c;
+                if (lane == 0 && prev_ct == nct - 1) {
+                    write_header(a, eb, tov | povf, excl + tot);
+                    if (a.boff) {
+                        // the total closes the offset table; zero its 16-byte pad
+                        a.boff[a.nb] = excl + tot;
+                        for (uint32_t i = a.nb + 1; i < (uint32_t)(pad16(4ull * (a.nb + 1)) / 4); ++i) a.boff[i] = 0;
                     }
                 }
             }
@@ -565,13 +681,11 @@ __global__ void __launch_bounds__(kCompressWarps * 32, 3) k_compress(const Compr
         __syncthreads();
         // ---- tile k-1: block offset table and compacted 128-bit stores ----
         if (k > 0) {
-            const uint32_t pb = buf ^ 1u;
-            const uint32_t t  = s_tile[pb] * kCompressWarps + wid;
+            const uint32_t t = prev_ct * kCompressWarps + wid;
             if (t < a.nb) {
-                uint32_t pre = s_excl;
-                for (uint32_t w2 = 0; w2 < wid; ++w2) pre += s_cnt[pb][w2];
+                uint32_t pre = s_pre[wid];
                 if (a.boff && lane == 0) a.boff[t] = pre;
-                const uint32_t* smp = dsm + (pb * kCompressWarps + wid) * kBlockWords;
+                const uint32_t* smp = dsm + ((buf ^ 1u) * kCompressWarps + wid) * kBlockWords;
                 uint4*          B   = reinterpret_cast<uint4*>(a.out + a.off_b);
                 const uint32_t  lt  = lanemask_lt();
 #pragma unroll
@@ -585,8 +699,7 @@ __global__ void __launch_bounds__(kCompressWarps * 32, 3) k_compress(const Compr
         if (!have) break;  // uniform; tile k-1 (if any) has been resolved above
 #pragma unroll
         for (int i = 0; i < 8; ++i) bm_prev[i] = bm[i];
-        // the next iteration rewrites slot and buffer k+1 & 1, which phase E just read
-        __syncthreads();
+        prev_ct = ct;
     }
 }
 
