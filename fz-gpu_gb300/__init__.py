@@ -68,7 +68,11 @@ COMPRESS, DECOMPRESS = 0, 1
 class Request(C.Structure):
     _fields_ = [("id", C.c_uint64), ("dir", C.c_int), ("src", C.c_void_p), ("dst", C.c_void_p),
                 ("n", C.c_uint64), ("dims", Dims), ("eb", C.c_double), ("eb_mode", C.c_int),
-                ("mode", C.c_int), ("dst_capacity", C.c_uint64), ("src_bytes", C.c_uint64)]
+                ("mode", C.c_int), ("dst_capacity", C.c_uint64), ("src_bytes", C.c_uint64),
+                ("flags", C.c_uint32), ("header", C.POINTER(Header))]
+
+
+REQUEST_DEVICE = 1  # FZ_REQUEST_DEVICE: src and dst are device pointers
 
 
 class Completion(C.Structure):
@@ -426,7 +430,8 @@ class Batch:
 # ------------------------------------------------------------------ serving
 class Server:
     """Request loop with continuous batching under an HBM budget (fz_server_*).
-    Requests use host buffers; keep them alive until their completion is polled."""
+    Requests use host buffers, or device buffers with device=True (FZ_REQUEST_DEVICE);
+    keep them alive until their completion is polled."""
 
     def __init__(self, hbm_budget, slots, max_n):
         h = C.c_void_p()
@@ -435,9 +440,12 @@ class Server:
         self._out = (Completion * 256)()
 
     def submit(self, rid, direction, src, dst, dst_capacity, n=0, dims=(1, 1, 1), eb=0.0, rel=True,
-               mode=MODE_SIDECAR, src_bytes=0):
+               mode=MODE_SIDECAR, src_bytes=0, device=False, header=None):
+        """``header``: the Header of a device-resident stream to decompress (saves the
+        server a header fetch); fz_server_submit copies the request and the header."""
         r = Request(int(rid), int(direction), src, dst, int(n), _dims(dims), float(eb),
-                    EB_REL if rel else EB_ABS, int(mode), int(dst_capacity), int(src_bytes))
+                    EB_REL if rel else EB_ABS, int(mode), int(dst_capacity), int(src_bytes),
+                    REQUEST_DEVICE if device else 0, C.pointer(header) if header is not None else None)
         _check("fz_server_submit", lib().fz_server_submit(self.handle, C.byref(r)))
 
     def poll(self):

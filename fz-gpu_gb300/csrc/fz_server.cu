@@ -5,8 +5,10 @@
 //   * a device pool of `hbm_budget` bytes (one allocation, first-fit free list with
 //     coalescing) from which each admitted request takes its input and output buffers;
 //   * `slots` execution slots, each a CUDA stream with its own workspace (scan state),
-//     a pinned 128-byte readback buffer and two events.
-// Requests (host buffers; pinned ones let the copies overlap) wait in a FIFO.
+//     a pinned 128-byte readback buffer and an event.
+// Requests wait in a FIFO.  Host-buffer requests (pinned ones let the copies overlap)
+// are staged through pool buffers; device-resident requests (FZ_REQUEST_DEVICE) run on
+// the caller's device buffers and only count their bytes against the pool.
 // fz_server_poll never blocks: it retires requests whose work has finished, then admits
 // queued requests while a slot is free and the pool can hold their buffers.  Requests
 // on different slots overlap on the device (copies on the copy engines, kernels
@@ -69,7 +71,9 @@ private:
     uint64_t                     used_ = 0;
 };
 
-enum class Phase { Idle, WaitHeader, WaitDone };
+// WaitInHeader: a device-resident decompression waits for its stream header (64 B);
+// WaitHeader: a compression waits for its output header (stream length).
+enum class Phase { Idle, WaitInHeader, WaitHeader, WaitDone };
 
 struct Slot {
     cudaStream_t  stream = nullptr;
@@ -78,6 +82,7 @@ struct Slot {
     cudaEvent_t   ev     = nullptr;
     Phase         phase  = Phase::Idle;
     fz_request    req{};
+    fz_header     hdr{};  // copy of req.header (req.header points at it while it runs)
     uint64_t      src_off = 0, src_bytes = 0, dst_off = 0, dst_bytes = 0;
     uint64_t      result  = 0;
     fz_status     status  = FZ_SUCCESS;
@@ -91,27 +96,42 @@ uint64_t max_stream_bytes(uint64_t n, fz_dims d, fz_mode m)
 
 }  // namespace
 
+// A queued request with its own copy of the caller's header (if any).
+struct Queued {
+    fz_request r;  // r.header is null here; has_header says whether h holds a copy
+    fz_header  h;
+    bool       has_header;
+};
+
 struct fz_server {
     uint8_t*                   d_pool = nullptr;
     Pool*                      pool   = nullptr;
     uint64_t                   budget = 0, max_n = 0;
     std::vector<Slot>          slots;
-    std::deque<fz_request>     queue;
+    std::deque<Queued>         queue;
     std::deque<fz_completion>  done;  // finished but not yet handed out
 };
 
 namespace {
 
+bool is_device(const fz_request& r) { return (r.flags & FZ_REQUEST_DEVICE) != 0; }
+
+// Pool bytes a request holds while it runs: its staging buffers, or for a device-resident
+// request the size of its own input and output.
 bool request_bytes(const fz_request& r, uint64_t* src, uint64_t* dst)
 {
     if (r.dir == FZ_COMPRESS) {
         *src = 4 * r.n;
-        *dst = max_stream_bytes(r.n, r.dims, r.mode);
+        *dst = is_device(r) ? r.dst_capacity : max_stream_bytes(r.n, r.dims, r.mode);
         return *dst != 0;
+    }
+    *src = r.src_bytes;
+    if (is_device(r)) {
+        *dst = r.dst_capacity;
+        return true;
     }
     fz_header h;
     std::memcpy(&h, r.src, sizeof(h));
-    *src = r.src_bytes;
     *dst = 4 * h.n;
     return true;
 }
@@ -124,39 +144,61 @@ void finish(fz_server* S, Slot& sl, fz_status st, uint64_t result)
     sl.phase = Phase::Idle;
 }
 
+// Decompression of a stream whose header is known, into the slot's output buffer, then
+// the status word (and for host requests the copy out).
+fz_status issue_decompress(fz_server* S, Slot& sl, const fz_header& h)
+{
+    const bool  dev   = is_device(sl.req);
+    const void* d_src = dev ? sl.req.src : S->d_pool + sl.src_off;
+    float*      d_dst = reinterpret_cast<float*>(dev ? sl.req.dst : S->d_pool + sl.dst_off);
+    if (4 * h.n > sl.req.dst_capacity) return FZ_OUT_OF_SPACE;
+    fz_status st = fz_decompress(sl.ws, d_src, sl.req.src_bytes, &h, d_dst, h.n, reinterpret_cast<fz_stream_t>(sl.stream));
+    if (st == FZ_SUCCESS && !dev &&
+        cudaMemcpyAsync(sl.req.dst, d_dst, 4 * h.n, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+        st = FZ_FAIL_GPU_MEMCPY;
+    if (st == FZ_SUCCESS && cudaMemcpyAsync(sl.h_buf + 64, sl.ws->status, 4, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+        st = FZ_FAIL_GPU_MEMCPY;
+    if (st == FZ_SUCCESS && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
+    sl.result = h.n;
+    sl.phase  = Phase::WaitDone;
+    return st;
+}
+
 // Enqueues a request's copies and kernels on a free slot.
 void issue(fz_server* S, Slot& sl, const fz_request& r, uint64_t src_off, uint64_t src_b, uint64_t dst_off,
            uint64_t dst_b)
 {
     sl.req = r, sl.src_off = src_off, sl.src_bytes = src_b, sl.dst_off = dst_off, sl.dst_bytes = dst_b;
-    uint8_t*    d_src = S->d_pool + src_off;
-    uint8_t*    d_dst = S->d_pool + dst_off;
+    const bool  dev   = is_device(r);
+    uint8_t*    d_src = dev ? (uint8_t*)r.src : S->d_pool + src_off;
+    uint8_t*    d_dst = dev ? (uint8_t*)r.dst : S->d_pool + dst_off;
     fz_stream_t hs    = reinterpret_cast<fz_stream_t>(sl.stream);
-    cudaError_t e     = cudaMemcpyAsync(d_src, r.src, src_b, cudaMemcpyHostToDevice, sl.stream);
-    fz_status   st    = e == cudaSuccess ? FZ_SUCCESS : FZ_FAIL_GPU_MEMCPY;
+    fz_status   st    = FZ_SUCCESS;
+    if (!dev && cudaMemcpyAsync(d_src, r.src, src_b, cudaMemcpyHostToDevice, sl.stream) != cudaSuccess)
+        st = FZ_FAIL_GPU_MEMCPY;
     if (r.dir == FZ_COMPRESS) {
         if (st == FZ_SUCCESS)
             st = fz_compress(sl.ws, reinterpret_cast<const float*>(d_src), r.n, r.dims, r.eb, r.eb_mode, r.mode,
-                             d_dst, dst_b, nullptr, hs);
+                             d_dst, dev ? r.dst_capacity : dst_b, nullptr, hs);
         // header and status come back first; the stream's length follows from nnz
         if (st == FZ_SUCCESS && cudaMemcpyAsync(sl.h_buf, d_dst, 64, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
             st = FZ_FAIL_GPU_MEMCPY;
         if (st == FZ_SUCCESS && cudaMemcpyAsync(sl.h_buf + 64, sl.ws->status, 4, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
             st = FZ_FAIL_GPU_MEMCPY;
+        if (st == FZ_SUCCESS && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
         sl.phase = Phase::WaitHeader;
+    } else if (dev && sl.req.header) {
+        if (st == FZ_SUCCESS) st = issue_decompress(S, sl, sl.hdr);
+    } else if (dev) {
+        // the header lives on the device: fetch it first (fz_server_poll never blocks)
+        if (cudaMemcpyAsync(sl.h_buf, d_src, 64, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess) st = FZ_FAIL_GPU_MEMCPY;
+        if (st == FZ_SUCCESS && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
+        sl.phase = Phase::WaitInHeader;
     } else {
         fz_header h;
         std::memcpy(&h, r.src, sizeof(h));
-        if (st == FZ_SUCCESS)
-            st = fz_decompress(sl.ws, d_src, r.src_bytes, &h, reinterpret_cast<float*>(d_dst), h.n, hs);
-        if (st == FZ_SUCCESS && cudaMemcpyAsync(r.dst, d_dst, 4 * h.n, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
-            st = FZ_FAIL_GPU_MEMCPY;
-        if (st == FZ_SUCCESS && cudaMemcpyAsync(sl.h_buf + 64, sl.ws->status, 4, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
-            st = FZ_FAIL_GPU_MEMCPY;
-        sl.result = h.n;
-        sl.phase  = Phase::WaitDone;
+        if (st == FZ_SUCCESS) st = issue_decompress(S, sl, h);
     }
-    if (st == FZ_SUCCESS && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
     if (st != FZ_SUCCESS) {
         cudaStreamSynchronize(sl.stream);
         finish(S, sl, st, 0);
@@ -211,7 +253,10 @@ fz_status fz_server_submit(fz_server* S, const fz_request* r)
     if (!S || !r || !r->src || !r->dst) return FZ_INVALID_ARG;
     if (r->dir != FZ_COMPRESS && r->dir != FZ_DECOMPRESS) return FZ_INVALID_ARG;
     if (r->dir == FZ_DECOMPRESS && r->src_bytes < FZ_HEADER_BYTES) return FZ_INVALID_ARG;
-    S->queue.push_back(*r);
+    Queued q{*r, {}, r->header != nullptr};
+    if (q.has_header) q.h = *r->header;
+    q.r.header = nullptr;  // re-pointed at the slot's copy when the request is issued
+    S->queue.push_back(q);
     return FZ_SUCCESS;
 }
 
@@ -227,6 +272,16 @@ fz_status fz_server_poll(fz_server* S, fz_completion* out, uint32_t max, uint32_
             finish(S, sl, FZ_FAIL_GPU_ILLEGAL_ACCESS, 0);
             continue;
         }
+        if (sl.phase == Phase::WaitInHeader) {
+            fz_header h;
+            std::memcpy(&h, sl.h_buf, sizeof(h));
+            const fz_status st = issue_decompress(S, sl, h);
+            if (st != FZ_SUCCESS) {
+                cudaStreamSynchronize(sl.stream);
+                finish(S, sl, st, 0);
+            }
+            continue;
+        }
         if (sl.phase == Phase::WaitHeader) {
             fz_header h;
             std::memcpy(&h, sl.h_buf, sizeof(h));
@@ -234,8 +289,11 @@ fz_status fz_server_poll(fz_server* S, fz_completion* out, uint32_t max, uint32_
             fz_status st    = status_word(sl);
             if (st == FZ_SUCCESS) st = fz_stream_bytes(&h, &bytes);
             if (st == FZ_SUCCESS && bytes > sl.req.dst_capacity) st = FZ_OUT_OF_SPACE;
-            if (st == FZ_SUCCESS &&
-                cudaMemcpyAsync(sl.req.dst, S->d_pool + sl.dst_off, bytes, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+            if (st != FZ_SUCCESS || is_device(sl.req)) {  // a device result is in place already
+                finish(S, sl, st, st == FZ_SUCCESS ? bytes : 0);
+                continue;
+            }
+            if (cudaMemcpyAsync(sl.req.dst, S->d_pool + sl.dst_off, bytes, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
                 st = FZ_FAIL_GPU_MEMCPY;
             if (st == FZ_SUCCESS && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
             if (st != FZ_SUCCESS) {
@@ -257,9 +315,13 @@ fz_status fz_server_poll(fz_server* S, fz_completion* out, uint32_t max, uint32_
                 break;
             }
         if (!free_slot) break;
-        const fz_request r = S->queue.front();
+        const Queued     qf = S->queue.front();
+        fz_request       r  = qf.r;
         uint64_t         sb = 0, db = 0;
-        const uint64_t   n  = r.dir == FZ_COMPRESS ? r.n : reinterpret_cast<const fz_header*>(r.src)->n;
+        // a device-resident stream's element count is only known once its header is read
+        // (fz_decompress checks it against the slot's workspace and dst_capacity then)
+        const bool     dev_dec = r.dir == FZ_DECOMPRESS && is_device(r);
+        const uint64_t n = r.dir == FZ_COMPRESS ? r.n : dev_dec ? 0 : reinterpret_cast<const fz_header*>(r.src)->n;
         const bool small_dst = r.dir == FZ_DECOMPRESS && 4 * n > r.dst_capacity;
         if (!request_bytes(r, &sb, &db) || n > S->max_n || small_dst || sb + db + 512 > S->budget) {
             S->queue.pop_front();  // can never run
@@ -273,6 +335,8 @@ fz_status fz_server_poll(fz_server* S, fz_completion* out, uint32_t max, uint32_
             break;
         }
         S->queue.pop_front();
+        free_slot->hdr = qf.h;
+        if (qf.has_header) r.header = &free_slot->hdr;
         issue(S, *free_slot, r, so, sb, dof, db);
     }
     uint32_t k = 0;

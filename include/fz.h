@@ -282,6 +282,11 @@ fz_status fz_batch_destroy(fz_batch* batch);
    Decompression: src the stream (src_bytes; its header is read from src) -> dst float[n]
    (dst_capacity bytes, at least 4n).  A request that can never run (larger than the
    budget or than max_n, or dst too small) completes with FZ_OUT_OF_SPACE/FZ_INVALID_ARG. */
+/* fz_request.flags: src and dst are device pointers (the field already lives in HBM and
+   the result stays there); without it both are host pointers (pinned ones let the
+   copies overlap) and the server stages them through its pool. */
+#define FZ_REQUEST_DEVICE 1u
+
 typedef struct fz_request {
     uint64_t     id;           /* the caller's tag, echoed in the completion */
     fz_direction dir;
@@ -292,8 +297,11 @@ typedef struct fz_request {
     double       eb;
     fz_eb_mode   eb_mode;
     fz_mode      mode;
-    uint64_t     dst_capacity;
+    uint64_t     dst_capacity; /* bytes */
     uint64_t     src_bytes;
+    uint32_t     flags;        /* FZ_REQUEST_DEVICE or 0 */
+    const fz_header* header;   /* decompression of a device-resident stream: its header on
+                                  the host, or null to have the server fetch it first */
 } fz_request;
 
 typedef struct fz_completion {
@@ -304,7 +312,8 @@ typedef struct fz_completion {
 
 /* A request loop with continuous batching under an HBM budget: `slots` streams, each with
    its own workspace, share one device pool of hbm_budget bytes from which every admitted
-   request takes its input and output buffers.  Requests queue in arrival order;
+   host-buffer request takes its input and output buffers (a device-resident request
+   counts its input and output bytes against the same budget).  Requests queue in arrival order;
    fz_server_poll (non-blocking) retires finished requests and admits queued ones as
    slots and pool memory free up, so requests that arrive while others run overlap on
    the device.  No counterpart in the reference (one field per process, fz.cu:226-238). */

@@ -67,3 +67,61 @@ def test_request_larger_than_the_budget_is_rejected(fz, synth):
                                   dst_capacity=out.numel(), n=d.size, dims=(600, 600, 1), eb=1e-3)])
     assert done[7][0] == fz.OUT_OF_SPACE
     server.close()
+
+
+@pytest.mark.parametrize("budget_mb,slots", [(512, 4), (12, 3)])
+def test_device_resident_requests_match_and_mix_with_host_ones(fz, synth, budget_mb, slots):
+    """FZ_REQUEST_DEVICE: fields already in HBM compress into device streams and decompress
+    back in place; the streams equal fz_compress's and the reconstructions equal
+    fz_decompress's, alone and interleaved with host-buffer requests."""
+    items = _fields(synth)
+    ws = fz.Workspace(max(d.size for d, _, _ in items))
+    xd = [torch.from_numpy(d).cuda() for d, _, _ in items]
+    alone = [fz.compress(x, dims, eb, ws=ws) for x, (_, dims, eb) in zip(xd, items)]
+    alone_rec = [fz.decompress(s, ws=ws) for s in alone]
+    caps = [fz.max_compressed_bytes(d.size, dims) for d, dims, _ in items]
+    sd = [torch.zeros(c, dtype=torch.uint8, device="cuda") for c in caps]
+    rd = [torch.zeros(d.size, dtype=torch.float32, device="cuda") for d, _, _ in items]
+    hst = [torch.from_numpy(s.cpu().numpy()).pin_memory() for s in alone]
+    hrec = [torch.empty(d.size, dtype=torch.float32).pin_memory() for d, _, _ in items]
+    rd2 = [torch.zeros(d.size, dtype=torch.float32, device="cuda") for d, _, _ in items]
+    reqs = []
+    for i, (d, dims, eb) in enumerate(items):
+        # compress in HBM; decompress in HBM with the header fetched by the server or given
+        # on the host (a copy made at submit: the Header object is dropped right away);
+        # decompress from host buffers
+        reqs.append(dict(rid=4 * i, direction=fz.COMPRESS, src=xd[i].data_ptr(), dst=sd[i].data_ptr(),
+                         dst_capacity=caps[i], n=d.size, dims=dims, eb=eb, device=True))
+        reqs.append(dict(rid=4 * i + 1, direction=fz.DECOMPRESS, src=alone[i].data_ptr(), dst=rd[i].data_ptr(),
+                         dst_capacity=4 * d.size, src_bytes=alone[i].numel(), device=True))
+        reqs.append(dict(rid=4 * i + 2, direction=fz.DECOMPRESS, src=hst[i].data_ptr(), dst=hrec[i].data_ptr(),
+                         dst_capacity=4 * d.size, src_bytes=alone[i].numel()))
+        reqs.append(dict(rid=4 * i + 3, direction=fz.DECOMPRESS, src=alone[i].data_ptr(), dst=rd2[i].data_ptr(),
+                         dst_capacity=4 * d.size, src_bytes=alone[i].numel(), device=True,
+                         header=fz.parse_header(alone[i][:64].cpu().numpy())))
+    server = fz.Server(budget_mb << 20, slots, max(d.size for d, _, _ in items))
+    done = _run(fz, server, reqs)
+    torch.cuda.synchronize()
+    for i, (d, _, _) in enumerate(items):
+        st, nb = done[4 * i]
+        assert st == fz.SUCCESS and nb == alone[i].numel()
+        assert torch.equal(sd[i][:nb], alone[i])
+        for k, rec in ((1, rd[i].cpu()), (2, hrec[i]), (3, rd2[i].cpu())):
+            st, nb = done[4 * i + k]
+            assert st == fz.SUCCESS and nb == d.size
+            assert np.array_equal(rec.numpy().view(np.uint32), alone_rec[i].cpu().numpy().view(np.uint32))
+    assert server.pending() == (0, 0, 0)
+    server.close()
+
+
+def test_device_request_with_short_output_fails_cleanly(fz, synth):
+    d = synth.smooth2d(300, 200, seed=48)
+    x = torch.from_numpy(d).cuda()
+    st_t = fz.compress(x, (300, 200, 1), 1e-3)
+    out = torch.zeros(d.size - 1, dtype=torch.float32, device="cuda")  # one element short
+    server = fz.Server(64 << 20, 2, d.size)
+    done = _run(fz, server, [dict(rid=1, direction=fz.DECOMPRESS, src=st_t.data_ptr(), dst=out.data_ptr(),
+                                  dst_capacity=4 * out.numel(), src_bytes=st_t.numel(), device=True)])
+    assert done[1][0] == fz.OUT_OF_SPACE
+    assert server.pending() == (0, 0, 0)
+    server.close()
