@@ -398,8 +398,10 @@ __device__ __forceinline__ void codes4(const float* __restrict__ in, const Geo& 
 constexpr int kRangeUnroll = 8;
 // max and min of the field (fz.cu:137) as order-preserving integers folded with one
 // atomicMin/atomicMax per CTA into mm[0..1], which the consuming compress kernel resets
-// to "empty" for the next call.  kRangeUnroll 16-byte loads in flight per thread;
-// NaN/Inf raise kStatusNonfinite.
+// to "empty" for the next call.  Each thread issues kRangeUnroll 16-byte loads at once
+// (coalesced across the CTA); the grid covers the field in one batch per thread, so the
+// block scheduler keeps every SM streaming until the last CTAs.  NaN/Inf raise
+// kStatusNonfinite.
 __global__ void __launch_bounds__(256) k_range(const float* __restrict__ in, uint32_t n, uint32_t* mm,
                                                uint32_t* status)
 {
@@ -408,7 +410,6 @@ __global__ void __launch_bounds__(256) k_range(const float* __restrict__ in, uin
     uint32_t       nonfinite = 0;
     const uint32_t n4        = n / 4;
     const uint32_t per       = blockDim.x * kRangeUnroll;
-    // one resident wave; each pass keeps kRangeUnroll 16-byte loads in flight per thread
     for (uint32_t b = blockIdx.x * per + threadIdx.x; b < n4; b += gridDim.x * per) {
         float4 v[kRangeUnroll];
 #pragma unroll
@@ -733,9 +734,8 @@ static uint32_t resident_ctas(K kernel, int threads, int dyn_smem = 0)
 
 cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* status, cudaStream_t s)
 {
-    static const uint32_t wave = resident_ctas(k_range, 256);
-    const uint64_t        want = cdiv(n / 4, 256ull * kRangeUnroll);
-    const uint32_t        ctas = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, wave));
+    const uint64_t want = cdiv(n / 4, 256ull * kRangeUnroll);  // n < 2^31: at most 2^18 CTAs
+    const uint32_t ctas = (uint32_t)std::max<uint64_t>(1, want);
     k_range<<<ctas, 256, 0, s>>>(in, n, mm, status);
     return cudaGetLastError();
 }
