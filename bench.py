@@ -12,7 +12,9 @@ is visited once per step, so each step reads its inputs from HBM.
   value      uncompressed GB/s through the codec, both directions:
              steps * fields * 2 * 4n bytes / device time (CUDA events), summed over ranks
   e2e        the same metric through the host-buffer C-ABI calls fz_compress_host /
-             fz_decompress_host (pinned host memory, H2D and D2H copies inside the region)
+             fz_decompress_host (pinned host memory, H2D and D2H copies inside the region),
+             issued from eight host threads with a workspace each so that one field's
+             input copy overlaps another's output copy on the host link
   roofline   the dominant kernel's algorithmic bytes per launch / its mean event-timed
              launch duration, against the measured HBM copy bandwidth
   cpu_baseline  the oracle (C, OpenMP) on this host's cores, round trips of one field
@@ -362,50 +364,80 @@ def run_fz(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+# host threads issuing e2e round trips (one per field of a step): with several in flight
+# the host link carries H2D and D2H at once (measured 210 + 193 GB/s one-way, 339 both)
+E2E_THREADS = int(os.environ.get("FZ_E2E_THREADS", "8"))
+
+
 def e2e(fz, L, fields, n, cap, sizes, args, dev, world, dist):
-    """Host-buffer round trips through fz_compress_host / fz_decompress_host."""
+    """Host-buffer round trips through fz_compress_host / fz_decompress_host, issued
+    from E2E_THREADS host threads, each with its own workspace, stream and pinned
+    staging buffers (the calls release the GIL), so one field's input copy (H2D) runs
+    beside another's output copy (D2H)."""
+    import threading
     import numpy as np
     import torch
     steps = min(args.steps, 30)
     hin = [torch.from_numpy(f).pin_memory() for f in fields]
-    hst = torch.empty(cap, dtype=torch.uint8).pin_memory()
-    hout = torch.empty(n, dtype=torch.float32).pin_memory()
-    ws = fz.Workspace(n)
     dims = fz._dims(DIMS)
-    sh = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    workers = []
+    for _ in range(E2E_THREADS):
+        workers.append({"ws": fz.Workspace(n), "st": torch.cuda.Stream(dev),
+                        "hst": torch.empty(cap, dtype=torch.uint8).pin_memory(),
+                        "hout": torch.empty(n, dtype=torch.float32).pin_memory(), "bytes": 0, "err": None})
 
-    def one(i):
+    def one(w, i):
         nb = C.c_uint64()
-        st = L.fz_compress_host(ws.handle, C.c_void_p(hin[i].data_ptr()), n, dims, EB, fz.EB_REL,
-                                fz.MODE_SIDECAR, C.c_void_p(hst.data_ptr()), cap, C.byref(nb), sh)
-        st |= L.fz_decompress_host(ws.handle, C.c_void_p(hst.data_ptr()), nb.value,
-                                   C.c_void_p(hout.data_ptr()), n, sh)
+        sh = C.c_void_p(w["st"].cuda_stream)
+        st = L.fz_compress_host(w["ws"].handle, C.c_void_p(hin[i].data_ptr()), n, dims, EB, fz.EB_REL,
+                                fz.MODE_SIDECAR, C.c_void_p(w["hst"].data_ptr()), cap, C.byref(nb), sh)
+        st |= L.fz_decompress_host(w["ws"].handle, C.c_void_p(w["hst"].data_ptr()), nb.value,
+                                   C.c_void_p(w["hout"].data_ptr()), n, sh)
         if st:
             raise fz.FzError("e2e", st)
         return nb.value
 
-    for i in range(min(3, len(fields))):
-        one(i)
+    items = steps * len(fields)
+
+    def run(k):
+        w = workers[k]
+        torch.cuda.set_device(dev)
+        try:
+            for j in range(k, items, E2E_THREADS):
+                w["bytes"] += one(w, j % len(fields))
+                w["last"] = j % len(fields)
+        except Exception as ex:  # surfaced after join
+            w["err"] = ex
+
+    for k, w in enumerate(workers):
+        one(w, k % len(fields))
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    total_stream = 0
-    for _ in range(steps):
-        for i in range(len(fields)):
-            total_stream += one(i)
+    th = [threading.Thread(target=run, args=(k,)) for k in range(E2E_THREADS)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
+    for w in workers:
+        if w["err"] is not None:
+            raise w["err"]
     if dist:
         t = torch.tensor([el], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         el = t.item()
-    last = fields[(steps * len(fields) - 1) % len(fields)]
-    err = float(np.max(np.abs(hout.numpy().astype(np.float64) - last)))
-    assert err <= 1e-3 * float(np.float32(last.max() - last.min())) * 1.001, err
+    for w in workers:
+        last = fields[w["last"]]
+        err = float(np.max(np.abs(w["hout"].numpy().astype(np.float64) - last)))
+        assert err <= 1e-3 * float(np.float32(last.max() - last.min())) * 1.001, err
+    total_stream = sum(w["bytes"] for w in workers)
     per_step_stream = total_stream / steps
     return {"value": round(len(fields) * 2 * 4 * n * steps * world / el / 1e9, 2), "unit": "GB/s",
-            "steps": steps, "h2d_bytes_per_step": int(len(fields) * 4 * n + per_step_stream),
+            "steps": steps, "host_threads": E2E_THREADS,
+            "h2d_bytes_per_step": int(len(fields) * 4 * n + per_step_stream),
             "d2h_bytes_per_step": int(per_step_stream + len(fields) * 4 * n)}
 
 

@@ -154,32 +154,42 @@ constexpr uint32_t kSpinLimit = 1u << 22;  // polls before a wait gives up (~0.3
 
 // Warp-cooperative decoupled look-back (single pass, Merrill & Garland 2016).
 // Tile `t` has published its aggregate already (unless t == 0).  Each round the warp
-// inspects a window of 128 predecessors -- lane l loads tiles t-1-4l .. t-4-4l -- so a
-// tile started next to a thousand others still finds an inclusive prefix in a few
-// rounds.  Returns the exclusive prefix (value) and the OR of the predecessors' ovf
-// bits in every lane.  A wait longer than kSpinLimit polls raises kStatusTimeout and
-// counts the missing tiles as 0, so no warp ever waits forever.
+// inspects a window of 32 W predecessors -- lane l loads tiles t-1-Wl .. t-W-Wl -- and
+// proceeds as soon as every tile nearer than the first inclusive prefix in the window
+// has published (tiles beyond it may still be running).  Returns the exclusive prefix
+// (value) and the OR of the predecessors' ovf bits in every lane.  A wait longer than
+// kSpinLimit polls raises kStatusTimeout and counts the missing tiles as 0, so no warp
+// ever waits forever.
+template <int W = 4>
 __device__ __forceinline__ void lookback(const uint64_t* state, uint32_t t, uint32_t epoch,
                                          uint32_t* status, uint32_t& excl, uint32_t& ovf)
 {
-    const uint32_t lane = threadIdx.x & 31;
-    uint32_t       acc = 0, acc_ovf = 0;
-    int64_t        base    = (int64_t)t - 1 - 4 * (int64_t)lane;
-    uint32_t       spins   = 0;
-    bool           gave_up = false;
+    static_assert(W >= 1 && W <= 32, "window per lane");
+    constexpr uint32_t kAllW = W == 32 ? 0xFFFFFFFFu : (1u << W) - 1u;
+    const uint32_t     lane  = threadIdx.x & 31;
+    uint32_t           acc = 0, acc_ovf = 0;
+    int64_t            base  = (int64_t)t - 1 - W * (int64_t)lane;
+    uint32_t           spins = 0;
     while (true) {
-        uint64_t s[4];
-        bool     ready[4];
+        uint64_t s[W];
+        uint32_t rdy, inc;  // bit j: tile base-j has published / holds an inclusive prefix
+        int      first;     // first lane holding an inclusive prefix (32: none)
+        bool     gave_up = false;
         while (true) {
-            bool all = true;
+            rdy = 0, inc = 0;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
+            for (int j = 0; j < W; ++j) {
                 const int64_t pos = base - j;
-                s[j]     = pos >= 0 ? ld_state(state + pos) : state_pack(epoch, kFlagIncl, 0, 0);
-                ready[j] = (uint32_t)(s[j] >> 32) == epoch && state_flag(s[j]) != 0;
-                all      = all && ready[j];
+                s[j]         = pos >= 0 ? ld_state(state + pos) : state_pack(epoch, kFlagIncl, 0, 0);
+                const bool r = (uint32_t)(s[j] >> 32) == epoch && state_flag(s[j]) != 0;
+                rdy |= r ? (1u << j) : 0u;
+                inc |= (r && state_flag(s[j]) == kFlagIncl) ? (1u << j) : 0u;
             }
-            if (__all_sync(kFull, all)) break;
+            const uint32_t any = __ballot_sync(kFull, inc != 0);
+            first              = any ? __ffs(any) - 1 : 32;
+            // the tiles before the first inclusive prefix must all have published
+            const uint32_t need = (int)lane < first ? kAllW : ((int)lane == first ? (inc & (0u - inc)) - 1u : 0u);
+            if (__all_sync(kFull, (rdy & need) == need)) break;
             if (++spins > kSpinLimit) {
                 gave_up = true;
                 break;
@@ -188,26 +198,24 @@ __device__ __forceinline__ void lookback(const uint64_t* state, uint32_t t, uint
         }
         if (gave_up) {
             if (lane == 0) atomicOr(status, kStatusTimeout);
+            // not-ready tiles end the walk as an inclusive 0
 #pragma unroll
-            for (int j = 0; j < 4; ++j)  // not-ready tiles end the walk as an inclusive 0
-                if (!ready[j]) s[j] = state_pack(epoch, kFlagIncl, 0, 0);
+            for (int j = 0; j < W; ++j)
+                if (!((rdy >> j) & 1u)) s[j] = state_pack(epoch, kFlagIncl, 0, 0), inc |= 1u << j;
+            const uint32_t any = __ballot_sync(kFull, inc != 0);
+            first              = any ? __ffs(any) - 1 : 32;
         }
-        uint32_t mine = 0;  // bit j: tile base-j holds an inclusive prefix
-#pragma unroll
-        for (int j = 0; j < 4; ++j) mine |= (state_flag(s[j]) == kFlagIncl) ? (1u << j) : 0u;
-        const uint32_t any = __ballot_sync(kFull, mine != 0);
-        // lanes before the first lane holding a prefix take all 4 tiles; that lane
-        // takes its tiles up to its first prefix; later lanes take none
-        const int first = any ? __ffs(any) - 1 : 32;
-        const int jmax  = (int)lane < first ? 3 : ((int)lane == first ? __ffs(mine) - 1 : -1);
+        // lanes before the first lane holding a prefix take all W tiles; that lane takes
+        // its tiles up to its first prefix; later lanes take none
+        const int jmax = (int)lane < first ? W - 1 : ((int)lane == first ? __ffs(inc) - 1 : -1);
         uint32_t  v = 0, o = 0;
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < W; ++j)
             if (j <= jmax) v += state_value(s[j]), o |= state_ovf(s[j]);
         acc += __reduce_add_sync(kFull, v);
         acc_ovf |= __reduce_or_sync(kFull, o);
-        if (any) break;
-        base -= 128;
+        if (first < 32) break;
+        base -= 32 * W;
     }
     excl = acc;
     ovf  = acc_ovf;
