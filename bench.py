@@ -260,7 +260,10 @@ def run_fz(args, rank, world, local_rank):
 
     # Timed region 1 (value): the step replayed from CUDA graphs (fz_batch_create /
     # fz_batch_launch, one graph per direction).
-    gc, gd = fz.Batch(ws, comp, fz.COMPRESS), fz.Batch(ws, dec, fz.DECOMPRESS)
+    # autotuner: branch count per direction, timed on these fields (fz_batch_autotune)
+    bc, msc = fz.batch_autotune(ws, comp, fz.COMPRESS, reps=2, stream=stream)
+    bd, msd = fz.batch_autotune(ws, dec, fz.DECOMPRESS, reps=2, stream=stream)
+    gc, gd = fz.Batch(ws, comp, fz.COMPRESS, branches=bc), fz.Batch(ws, dec, fz.DECOMPRESS, branches=bd)
     for _ in range(args.warmup):
         gc.launch(stream), gd.launch(stream)
     torch.cuda.synchronize()
@@ -486,7 +489,10 @@ def run_batch(args, local_rank):
                              "dst_capacity": s_.numel()} for x, s_, n, (_, d, eb, _) in zip(X, S, ns, specs)])
     dec = fz.fields_array([{"src": s_.data_ptr(), "dst": y.data_ptr(), "src_bytes": b, "dst_capacity": y.numel(),
                             "header": h} for s_, y, b, h in zip(S, Y, sizes, heads)])
-    gc, gd = fz.Batch(ws, comp, fz.COMPRESS), fz.Batch(ws, dec, fz.DECOMPRESS)
+    # autotuner: branch count per direction, timed on these fields (fz_batch_autotune)
+    bc, msc = fz.batch_autotune(ws, comp, fz.COMPRESS, reps=2, stream=stream)
+    bd, msd = fz.batch_autotune(ws, dec, fz.DECOMPRESS, reps=2, stream=stream)
+    gc, gd = fz.Batch(ws, comp, fz.COMPRESS, branches=bc), fz.Batch(ws, dec, fz.DECOMPRESS, branches=bd)
     for _ in range(2):
         gc.launch(stream), gd.launch(stream)
     torch.cuda.synchronize()
@@ -507,9 +513,11 @@ def run_batch(args, local_rank):
             "speedup_vs_per_field": round(t_plain / t_batch, 2),
             "fields": len(specs), "total_gb": round(total / 1e9, 3), "steps": steps,
             "aggregate_ratio": round(ratio, 3), "higher_is_better": True,
+            "autotune": {"compress": {"branches": bc, "ms": {str(k): round(v, 3) for k, v in msc.items()}},
+                         "decompress": {"branches": bd, "ms": {str(k): round(v, 3) for k, v in msd.items()}}},
             "data": "synthetic (seeded device-side generators)",
             "config": {"workload": "mixed 1D/2D/3D, sizes log-uniform 64 KB-256 MB, eb in {1e-2,1e-3,1e-4}",
-                       "batched": "two CUDA-graph replays (fz_batch_launch)",
+                       "batched": "two CUDA-graph replays (fz_batch_launch), branch counts from fz_batch_autotune",
                        "per_field": "fz_compress with size readback + fz_decompress, one field at a time"}}
     print(json.dumps(line), flush=True)
 

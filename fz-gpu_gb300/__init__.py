@@ -113,6 +113,8 @@ SIGNATURES = {
     "fz_batch_create": (_I, [_P, _P, _U32, _I, _I, _I, C.POINTER(_P)]),
     "fz_batch_launch": (_I, [_P, _P]),
     "fz_batch_destroy": (_I, [_P]),
+    "fz_batch_create_ex": (_I, [_P, _P, _U32, _I, _I, _I, _U32, C.POINTER(_P)]),
+    "fz_batch_autotune": (_I, [_P, _P, _U32, _I, _I, _I, _U32, _P, C.POINTER(_U32), C.POINTER(C.c_double)]),
     "fz_server_create": (_I, [_U64, _U32, _U64, C.POINTER(_P)]),
     "fz_server_submit": (_I, [_P, C.POINTER(Request)]),
     "fz_server_poll": (_I, [_P, C.POINTER(Completion), _U32, C.POINTER(C.c_uint32)]),
@@ -402,14 +404,25 @@ def decompress_batch(ws, fields, stream=None):
     _check("fz_decompress_batch", lib().fz_decompress_batch(ws.handle, fields, len(fields), _stream_handle(stream)))
 
 
-class Batch:
-    """A batch recorded once into a CUDA graph (fz_batch_create) and replayed."""
+def batch_autotune(ws, fields, direction, rel=True, mode=MODE_SIDECAR, reps=3, stream=None):
+    """fz_batch_autotune: (best branch count, {branches: mean replay ms}) for these fields."""
+    best, ms = C.c_uint32(), (C.c_double * 5)()
+    _check("fz_batch_autotune", lib().fz_batch_autotune(ws.handle, fields, len(fields), direction,
+                                                        EB_REL if rel else EB_ABS, mode, int(reps),
+                                                        _stream_handle(stream), C.byref(best), ms))
+    return best.value, {b: ms[i] for i, b in enumerate((1, 2, 4, 8, 16)) if ms[i] > 0}
 
-    def __init__(self, ws, fields, direction, rel=True, mode=MODE_SIDECAR):
+
+class Batch:
+    """A batch recorded once into a CUDA graph (fz_batch_create / fz_batch_create_ex with
+    `branches` parallel branches, 0 = default) and replayed."""
+
+    def __init__(self, ws, fields, direction, rel=True, mode=MODE_SIDECAR, branches=0):
         self.ws, self.fields = ws, fields  # keep the buffers' owners alive
         h = C.c_void_p()
-        _check("fz_batch_create", lib().fz_batch_create(ws.handle, fields, len(fields), direction,
-                                                        EB_REL if rel else EB_ABS, mode, C.byref(h)))
+        _check("fz_batch_create_ex", lib().fz_batch_create_ex(ws.handle, fields, len(fields), direction,
+                                                              EB_REL if rel else EB_ABS, mode, int(branches),
+                                                              C.byref(h)))
         self.handle = h
 
     def launch(self, stream=None):

@@ -637,18 +637,25 @@ struct fz_batch {
 extern "C" {
 
 // The batch is captured with parallel branches: fields go round-robin to up to
-// kBatchBranches forked streams, each with its own workspace (scan state, range
+// `branches` forked streams, each with its own workspace (scan state, range
 // accumulators), so the kernels of small fields run side by side.
 static constexpr uint32_t kBatchBranches = 8;
 
 fz_status fz_batch_create(fz_workspace* ws, const fz_field* fields, uint32_t count, fz_direction dir,
                           fz_eb_mode eb_mode, fz_mode mode, fz_batch** out)
 {
+    return fz_batch_create_ex(ws, fields, count, dir, eb_mode, mode, 0, out);
+}
+
+fz_status fz_batch_create_ex(fz_workspace* ws, const fz_field* fields, uint32_t count, fz_direction dir,
+                             fz_eb_mode eb_mode, fz_mode mode, uint32_t nbranch, fz_batch** out)
+{
     if (!ws || !out || (!fields && count) || (dir != FZ_COMPRESS && dir != FZ_DECOMPRESS)) return FZ_INVALID_ARG;
+    if (nbranch > FZ_BATCH_MAX_BRANCHES) return FZ_INVALID_ARG;
     *out = nullptr;
     fz_batch* b = new (std::nothrow) fz_batch();
     if (!b) return FZ_FAIL_GPU_MALLOC;
-    const uint32_t branches = std::max(1u, std::min(kBatchBranches, count));
+    const uint32_t branches = std::max(1u, std::min(nbranch ? nbranch : kBatchBranches, count));
     uint64_t       max_n    = 1;
     for (uint32_t i = 0; i < count; ++i) max_n = std::max<uint64_t>(max_n, dir == FZ_COMPRESS ? fields[i].n : fields[i].header.n);
     std::vector<fz_workspace*> wss{ws};
@@ -723,6 +730,47 @@ fz_status fz_batch_destroy(fz_batch* b)
     for (fz_workspace* w : b->own_ws) fz_workspace_destroy(w);
     delete b;
     return FZ_SUCCESS;
+}
+
+fz_status fz_batch_autotune(fz_workspace* ws, const fz_field* fields, uint32_t count, fz_direction dir,
+                            fz_eb_mode eb_mode, fz_mode mode, uint32_t reps, fz_stream_t stream,
+                            uint32_t* best, double* ms)
+{
+    if (!ws || !best || !count || !fields || !reps) return FZ_INVALID_ARG;
+    static constexpr uint32_t kCand[5] = {1, 2, 4, 8, 16};
+    cudaStream_t s  = reinterpret_cast<cudaStream_t>(stream);
+    cudaEvent_t  e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return FZ_FAIL_GPU_ILLEGAL_ACCESS;
+    }
+    fz_status st     = FZ_SUCCESS;
+    float     best_t = 0;
+    *best            = 0;
+    for (int c = 0; c < 5 && st == FZ_SUCCESS; ++c) {
+        if (ms) ms[c] = 0;
+        if (kCand[c] > count && c > 0) continue;  // the same graph as a smaller candidate
+        fz_batch* b = nullptr;
+        st          = fz_batch_create_ex(ws, fields, count, dir, eb_mode, mode, kCand[c], &b);
+        if (st != FZ_SUCCESS) break;
+        st = fz_batch_launch(b, stream);  // warm-up
+        cudaError_t e = st == FZ_SUCCESS ? cudaEventRecord(e0, s) : cudaSuccess;
+        for (uint32_t r = 0; r < reps && st == FZ_SUCCESS && e == cudaSuccess; ++r) st = fz_batch_launch(b, stream);
+        if (st == FZ_SUCCESS && e == cudaSuccess) e = cudaEventRecord(e1, s);
+        if (st == FZ_SUCCESS && e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float t = 0;
+        if (st == FZ_SUCCESS && e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+        if (st == FZ_SUCCESS && e != cudaSuccess) st = map_err(e);
+        if (st == FZ_SUCCESS) {
+            t /= (float)reps;
+            if (ms) ms[c] = t;
+            if (*best == 0 || t < best_t) *best = kCand[c], best_t = t;
+        }
+        fz_batch_destroy(b);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return st;
 }
 
 }  // extern "C"

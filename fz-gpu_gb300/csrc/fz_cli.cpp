@@ -23,6 +23,17 @@
 
 namespace {
 
+// The reference has no outlier channel (its codes are 16 bits): deltas that do not fit
+// are reported, on stderr so that stdout keeps the reference's three lines.
+void warn_overflow(const fz_header& h)
+{
+    if (h.flags & FZ_FLAG_CODE_OVERFLOW)
+        std::fprintf(stderr,
+                     "warning: some prediction deltas do not fit the 16-bit codes (|delta| >= 2^15, or "
+                     "non-finite input); the stream does not meet the error bound at those points "
+                     "(FZ_FLAG_CODE_OVERFLOW)\n");
+}
+
 int die(const char* what, fz_status st)
 {
     std::fprintf(stderr, "fz-gpu: %s: %s\n", what, fz_status_string(st));
@@ -102,6 +113,7 @@ int decompress_main(int argc, char** argv)
     s         = fz_decompress_host(ws, h_st, st.size(), h_out, h.n, nullptr);
     double t1 = now_s();
     if (s != FZ_SUCCESS) return die("decompress", s);
+    warn_overflow(h);
     if (!write_file(out, h_out, h.n * 4)) {
         std::fprintf(stderr, "fail to write %s\n", out.c_str());
         return 1;
@@ -201,6 +213,7 @@ int main(int argc, char** argv)
     std::printf("original size: %d\n", (int)orig);
     std::printf("compressed size: %d\n", (int)comp);
     std::printf("compression ratio: %f\n", (float)file_bytes / (float)comp);
+    warn_overflow(h);
     if (!out.empty() && !write_file(out, h_out, bytes)) {
         std::fprintf(stderr, "fail to write %s\n", out.c_str());
         return 1;

@@ -276,6 +276,24 @@ fz_status fz_batch_create(fz_workspace* ws, const fz_field* fields, uint32_t cou
 fz_status fz_batch_launch(fz_batch* batch, fz_stream_t stream);
 fz_status fz_batch_destroy(fz_batch* batch);
 
+/* The same with an explicit number of parallel branches (1..FZ_BATCH_MAX_BRANCHES; 0 =
+   the default of fz_batch_create, 8).  No counterpart in the reference. */
+#define FZ_BATCH_MAX_BRANCHES 16u
+fz_status fz_batch_create_ex(fz_workspace* ws, const fz_field* fields, uint32_t count,
+                             fz_direction dir, fz_eb_mode eb_mode, fz_mode mode, uint32_t branches,
+                             fz_batch** out);
+
+/* Autotuner for batch scheduling (no counterpart in the reference).  The stream format
+   fixes the shuffle block and the Lorenzo tiles, so what is tuned is how many fields run
+   side by side: captures the batch with 1, 2, 4, 8 and 16 branches (capped at `count`),
+   replays each `reps` times on `stream` (timed with CUDA events; the replays do the
+   batch's work, so its outputs are written) and returns the fastest branch count in
+   *best and, if ms is not null, each candidate's mean replay time in ms[0..4] (0 for
+   candidates above `count`). */
+fz_status fz_batch_autotune(fz_workspace* ws, const fz_field* fields, uint32_t count, fz_direction dir,
+                            fz_eb_mode eb_mode, fz_mode mode, uint32_t reps, fz_stream_t stream,
+                            uint32_t* best, double* ms);
+
 /* -------------------------------------------------------------- serving -- */
 /* A request on host buffers (pinned buffers let copies overlap with other requests).
    Compression: src float[n] with dims, eb, eb_mode, mode -> dst (dst_capacity bytes).

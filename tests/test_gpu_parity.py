@@ -314,3 +314,34 @@ def test_graph_batch_replays_are_exact(fz, oracle, synth):
             assert_same_stream(s[: w.size].cpu().numpy(), w)
             assert np.array_equal(y.cpu().numpy().view(np.uint32), oracle.decompress(w).view(np.uint32))
     assert ws.status() == fz.SUCCESS
+
+
+def test_batch_branch_counts_and_autotune(fz, oracle, synth):
+    """Every branch count gives the same streams and reconstructions; the autotuner
+    times the candidates on these fields and returns one of them."""
+    items = _mixed_fields(synth)
+    ws = fz.Workspace(max(d.size for d, _, _ in items))
+    xs, ss, ys, comp = _batch_buffers(fz, items)
+    wants = [oracle.compress(d, dims, eb) for d, dims, eb in items]
+    dec = fz.fields_array([{"src": s.data_ptr(), "dst": y.data_ptr(), "src_bytes": w.size, "dst_capacity": y.numel(),
+                            "header": fz.parse_header(w)} for s, y, w in zip(ss, ys, wants)])
+    for branches in (1, 3, 16):
+        g, gd = fz.Batch(ws, comp, fz.COMPRESS, branches=branches), fz.Batch(ws, dec, fz.DECOMPRESS, branches=branches)
+        for s in ss:
+            s.fill_(0xCD)
+        g.launch()
+        gd.launch()
+        torch.cuda.synchronize()
+        for s, y, w in zip(ss, ys, wants):
+            assert_same_stream(s[: w.size].cpu().numpy(), w)
+            assert np.array_equal(y.cpu().numpy().view(np.uint32), oracle.decompress(w).view(np.uint32))
+        g.close(), gd.close()
+    best, ms = fz.batch_autotune(ws, comp, fz.COMPRESS, reps=2)
+    assert best in ms and all(t > 0 for t in ms.values())
+    assert set(ms) <= {1, 2, 4, 8, 16} and 1 in ms
+    torch.cuda.synchronize()
+    for s, w in zip(ss, wants):  # the tuning replays wrote the same streams
+        assert_same_stream(s[: w.size].cpu().numpy(), w)
+    with pytest.raises(fz.FzError):
+        fz.Batch(ws, comp, fz.COMPRESS, branches=17)
+    assert ws.status() == fz.SUCCESS
