@@ -225,7 +225,7 @@ class Workspace:
         """Status of a look-back that waits on a tile nothing publishes (FZ_TIMEOUT)."""
         return lib().fz_selftest_wait_timeout(self.handle, _stream_handle(stream))
 
-    KERNELS = ("k_range", "k_compress", "k_offsets", "k_decode", "k_recon")
+    KERNELS = ("k_range", "k_compress", "k_offsets", "k_decode", "k_recon", "k_compact")
 
     def enable_timing(self, capacity):
         _check("fz_workspace_enable_timing", lib().fz_workspace_enable_timing(self.handle, int(capacity)))

@@ -215,6 +215,7 @@ fz_status fz_workspace_bytes(uint64_t max_n, uint64_t* bytes)
     b += 16;                        // range accumulators
     b += pad16(2 * max_n + 16);     // decode scratch
     b += pad16(4 * tiles + 4);      // block offsets
+    b += pad16(4 * (tiles / 512 + 2));  // chunk counts per 512 blocks
     *bytes = b;
     return FZ_SUCCESS;
 }
@@ -244,10 +245,13 @@ fz_status fz_workspace_create(uint64_t max_n, fz_workspace** out)
     ws->status  = ws->tickets + 4;
     ws->total   = ws->tickets + 5;
     ws->epoch   = ws->tickets + 6;
+    ws->ovfw    = ws->tickets + 7;
+    ws->done    = ws->tickets + 8;
     p += 64;
     ws->mm       = reinterpret_cast<uint32_t*>(p), p += 16;
     ws->codes    = reinterpret_cast<uint16_t*>(p), p += pad16(2 * max_n + 16);
-    ws->boff     = reinterpret_cast<uint32_t*>(p);
+    ws->boff     = reinterpret_cast<uint32_t*>(p), p += pad16(4ull * ws->max_tiles + 4);
+    ws->supers   = reinterpret_cast<uint32_t*>(p);
     e            = cudaMemset(ws->d_base, 0, bytes);
     if (e == cudaSuccess) {
         const uint32_t init[2] = {0xFFFFFFFFu, 0u};  // empty min/max
@@ -374,8 +378,14 @@ fz_status fz_compress(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims d
         a.ebh.range = a.ebh.vmin = a.ebh.vmax = 0.0f;
     }
     if (e == cudaSuccess) {
+        // two launches: per-block slots in the decode scratch (2 bytes per element, one 4 KiB
+        // slot per shuffle block) and per-block counts in the block-offset array
         KernelTimer t(ws, s, 1);
-        e = launch_compress(a, s);
+        e = launch_encode(a, reinterpret_cast<uint4*>(ws->codes), ws->boff, ws->supers, ws->ovfw, s);
+    }
+    if (e == cudaSuccess) {
+        KernelTimer t(ws, s, 5);
+        e = launch_compact(a, reinterpret_cast<const uint4*>(ws->codes), ws->boff, ws->supers, ws->ovfw, ws->done, s);
     }
     if (e != cudaSuccess) return map_err(e);
     if (out_bytes) {

@@ -704,6 +704,150 @@ __global__ void __launch_bounds__(kCompressWarps * 32, 3) k_compress(const Compr
     }
 }
 
+// ====================================================== two-kernel compress ==
+// The workspace path splits compression in two launches so that no warp ever waits for
+// a look-back:
+//   k_encode   one CTA per scan tile (8 shuffle blocks, one per warp), independent of
+//              all others: phases A-C of compute_block (codes, transpose, chunk flags,
+//              bitmap words, sidecar), then the block's non-zero chunks, compacted, into
+//              its own 4 KiB slot of the workspace scratch and its chunk count into
+//              counts[t].  Overflow bits are OR-ed into one word.
+//              Each block's count is also added into the sum of its super-tile (512
+//              blocks).
+//   k_compact  every block's exclusive chunk offset -- the super-tile sums before its
+//              super-tile plus the counts inside it before the block: all known, so no
+//              CTA waits for another --, the offset table, the move of every block's
+//              chunks from its slot to Section B, and (last CTA to finish) the header.
+// The stream bytes equal the fused kernel's.
+constexpr uint32_t kCompactBlocks = 32;   // shuffle blocks per k_compact CTA
+constexpr uint32_t kSuperBlocks   = 512;  // shuffle blocks per super-tile sum
+
+template <int ND>
+__global__ void __launch_bounds__(kCompressWarps * 32, 3) k_encode(const CompressArgs a, uint4* slots,
+                                                                    uint32_t* counts, uint32_t* supers,
+                                                                    uint32_t* ovfw)
+{
+    __shared__ __align__(16) uint32_t smem[kCompressWarps][kBlockWords];
+    __shared__ float s_r;
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0)
+        s_r = a.mm ? eb_from_range(ord2f(__ldcg(a.mm)), ord2f(__ldcg(a.mm + 1)), a.eb_rel).ebx2_r : a.ebh.ebx2_r;
+    __syncthreads();
+    Geo g;
+    g.nl = a.nl, g.x = a.x, g.y = a.y, g.xy = a.xy, g.lim = a.n;
+    g.dx = a.dx, g.dxy = a.dxy, g.al_x = a.al_x, g.al_xy = a.al_xy, g.al_xyx = a.al_xyx;
+    uint32_t*      signw = (ND == 1 && a.mode == 1) ? reinterpret_cast<uint32_t*>(a.out + a.off_sign) : nullptr;
+    const uint32_t t     = blockIdx.x * kCompressWarps + wid;
+    uint32_t       bm[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cnt = 0, ovf = 0;
+    compute_block<ND>(a, g, t, s_r, lane, smem[wid], signw, bm, cnt, ovf);  // warp-uniform t
+    if (t < a.nb) {
+        uint4*         S   = slots + (size_t)t * kChunks;
+        const uint32_t lt  = lanemask_lt();
+        uint32_t       pre = 0;
+#pragma unroll
+        for (uint32_t i = 0; i < 8; ++i) {
+            if ((bm[i] >> lane) & 1u)
+                S[pre + __popc(bm[i] & lt)] = *reinterpret_cast<const uint4*>(smem[wid] + (lane + 32 * i) * 4);
+            pre += __popc(bm[i]);
+        }
+        if (lane == 0) {
+            counts[t] = cnt;
+            if (cnt) atomicAdd(supers + t / kSuperBlocks, cnt);
+        }
+    }
+    if (ovf && lane == 0) atomicOr(ovfw, 1u);
+}
+
+// One CTA per kCompactBlocks blocks; no CTA waits for another.  The CTA's first offset is
+// the sum of the super-tile sums before its super-tile plus the counts of the blocks of
+// its super-tile before it (block reductions); warp 0 scans its 32 counts.  All threads
+// then move the CTA's chunks: output chunk q comes from block j = the last with
+// pre[j] <= q, four independent 16-byte loads in flight per thread.  The last CTA to
+// finish writes the header and the offset table's total, and leaves the super-tile
+// sums, the overflow word, the done counter and the range accumulators reset.
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red)
+{
+    v = __reduce_add_sync(kFull, v);
+    __syncthreads();  // red may still be read by a previous call
+    if ((threadIdx.x & 31u) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    return __reduce_add_sync(kFull, (threadIdx.x & 31u) < kCompressWarps ? red[threadIdx.x & 31u] : 0u);
+}
+
+__global__ void __launch_bounds__(256) k_compact(const CompressArgs a, const uint4* slots, const uint32_t* counts,
+                                                 uint32_t* supers, uint32_t* ovfw, uint32_t* done)
+{
+    static_assert(kCompactBlocks == 32 && kSuperBlocks % kCompactBlocks == 0, "one warp scans the CTA's counts");
+    __shared__ uint32_t s_red[kCompressWarps], s_tot, s_pre[kCompactBlocks], s_last;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, wid = tid >> 5;
+    const uint32_t b0 = blockIdx.x * kCompactBlocks, sup = b0 / kSuperBlocks;
+    uint32_t       acc = 0;
+    for (uint32_t i = tid; i < sup; i += blockDim.x) acc += __ldcg(supers + i);
+    for (uint32_t b = sup * kSuperBlocks + tid; b < b0; b += blockDim.x) acc += __ldcg(counts + b);
+    const uint32_t excl = block_sum(acc, s_red);
+    if (wid == 0) {
+        const uint32_t b = b0 + lane;
+        const uint32_t c = b < a.nb ? __ldcg(counts + b) : 0u;
+        uint32_t       v = c;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(kFull, v, o);
+            if (lane >= o) v += u;
+        }
+        s_pre[lane] = v - c;
+        if (lane == 31) s_tot = v;
+        if (a.boff && b < a.nb) a.boff[b] = excl + v - c;
+    }
+    __syncthreads();
+    const uint32_t tot = s_tot;
+    uint4*         B   = reinterpret_cast<uint4*>(a.out + a.off_b) + excl;
+    for (uint32_t q0 = tid; q0 < tot; q0 += 4 * 256) {
+        uint4    v[4];
+        uint32_t qq[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t q = q0 + u * 256;
+            qq[u]            = q;
+            if (q < tot) {
+                uint32_t j = 0;  // last block with pre[j] <= q (a block with no chunks never matches last)
+#pragma unroll
+                for (uint32_t step = 16; step; step >>= 1)
+                    if (s_pre[j + step] <= q) j += step;
+                v[u] = __ldcg(slots + (size_t)(b0 + j) * kChunks + (q - s_pre[j]));
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (qq[u] < tot) B[qq[u]] = v[u];
+    }
+    // the last CTA to finish: header, offset-table total, resets
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();  // this CTA's reads of the sums precede its count
+        s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const uint32_t nsup  = (uint32_t)cdiv(a.nb, kSuperBlocks);
+    uint32_t       total = 0;
+    for (uint32_t i = tid; i < nsup; i += blockDim.x) total += __ldcg(supers + i);
+    total = block_sum(total, s_red);
+    for (uint32_t i = tid; i < nsup; i += blockDim.x) supers[i] = 0;
+    if (tid == 0) {
+        const EbInfo eb = a.mm ? eb_from_range(ord2f(__ldcg(a.mm)), ord2f(__ldcg(a.mm + 1)), a.eb_rel) : a.ebh;
+        write_header(a, eb, __ldcg(ovfw), total);
+        if (a.boff) {
+            // the total closes the offset table; zero its 16-byte pad
+            a.boff[a.nb] = total;
+            for (uint32_t i = a.nb + 1; i < (uint32_t)(pad16(4ull * (a.nb + 1)) / 4); ++i) a.boff[i] = 0;
+        }
+        *ovfw = 0;
+        *done = 0;
+        if (a.mm) a.mm[0] = 0xFFFFFFFFu, a.mm[1] = 0u;  // empty range for the next call
+    }
+}
+
 // One warp looks back from tile 1 at tile 0, which nothing publishes in this epoch: the
 // bounded wait must give up and raise kStatusTimeout (fz_selftest_wait_timeout).
 __global__ void k_wait_selftest(const uint64_t* state, const uint32_t* epoch, uint32_t* status)
@@ -737,6 +881,26 @@ cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* st
     const uint64_t want = cdiv(n / 4, 256ull * kRangeUnroll);  // n < 2^31: at most 2^18 CTAs
     const uint32_t ctas = (uint32_t)std::max<uint64_t>(1, want);
     k_range<<<ctas, 256, 0, s>>>(in, n, mm, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_encode(const CompressArgs& a, uint4* slots, uint32_t* counts, uint32_t* supers, uint32_t* ovfw,
+                          cudaStream_t s)
+{
+    const uint32_t ctas = (uint32_t)cdiv(a.ntiles, kCompressWarps);
+    switch (a.ndim) {
+    case 1: k_encode<1><<<ctas, kCompressWarps * 32, 0, s>>>(a, slots, counts, supers, ovfw); break;
+    case 2: k_encode<2><<<ctas, kCompressWarps * 32, 0, s>>>(a, slots, counts, supers, ovfw); break;
+    default: k_encode<3><<<ctas, kCompressWarps * 32, 0, s>>>(a, slots, counts, supers, ovfw); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact(const CompressArgs& a, const uint4* slots, const uint32_t* counts, uint32_t* supers,
+                           uint32_t* ovfw, uint32_t* done, cudaStream_t s)
+{
+    const uint32_t ctas = (uint32_t)std::max<uint64_t>(1, cdiv(a.nb, kCompactBlocks));
+    k_compact<<<ctas, 256, 0, s>>>(a, slots, counts, supers, ovfw, done);
     return cudaGetLastError();
 }
 

@@ -64,7 +64,13 @@ struct ReconArgs {
 
 // launchers (return the launch error)
 cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* status, cudaStream_t s);
-cudaError_t launch_compress(const CompressArgs& a, cudaStream_t s);
+cudaError_t launch_compress(const CompressArgs& a, cudaStream_t s);  // fused, single launch
+// two launches with per-block slots in a scratch of 4 KiB per shuffle block (workspace path);
+// supers: chunk counts per 512 blocks (zero on entry, left zero), done: a zero word
+cudaError_t launch_encode(const CompressArgs& a, uint4* slots, uint32_t* counts, uint32_t* supers, uint32_t* ovfw,
+                          cudaStream_t s);
+cudaError_t launch_compact(const CompressArgs& a, const uint4* slots, const uint32_t* counts, uint32_t* supers,
+                           uint32_t* ovfw, uint32_t* done, cudaStream_t s);
 cudaError_t launch_offsets(const uint8_t* st, uint64_t off_a, uint32_t nb, uint32_t nwords, uint64_t nnz,
                            uint32_t* boff, uint64_t* state, uint32_t* ticket, uint32_t* status,
                            uint32_t* epoch, cudaStream_t s);

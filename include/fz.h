@@ -147,10 +147,10 @@ fz_status fz_workspace_status(fz_workspace* ws, fz_stream_t stream);
    by a call on this workspace (up to `capacity` launches in total) is bracketed by a
    pair of CUDA events on the call's stream.  capacity 0 disables it. */
 fz_status fz_workspace_enable_timing(fz_workspace* ws, uint32_t capacity);
-/* Number of recorded launches of one kernel kind (0 range pass, 1 fused compress,
-   2 block offsets, 3 decode -- fused with the inverse Lorenzo for 1D and for 2D rows
-   of a multiple of 4 elements --, 4 separate inverse Lorenzo) and their summed
-   duration; syncs on the last recorded event and frees those records. */
+/* Number of recorded launches of one kernel kind (0 range pass, 1 compress -- codes,
+   bitshuffle, flags and per-block compaction --, 2 block offsets, 3 decode -- fused with
+   the inverse Lorenzo --, 4 separate inverse Lorenzo, 5 compaction scan and move) and
+   their summed duration; syncs on the last recorded event and frees those records. */
 fz_status fz_workspace_kernel_time(fz_workspace* ws, int kind, uint32_t* launches,
                                    double* total_ms);
 
