@@ -132,44 +132,54 @@ __device__ __forceinline__ uint32_t swz(uint32_t q)
     return ((g << 3) | (t ^ (g & 7u))) << 2;
 }
 
+// Position (row, col) of element e0 + 128 given that of e0 (x a multiple of 4).
+__device__ __forceinline__ void advance128(const Geo& g, uint32_t e0, uint32_t& row, uint32_t& col)
+{
+    if (g.x >= 128) {
+        col += 128;
+        if (col >= g.x) col -= g.x, ++row;
+    } else {
+        row = fdiv(e0 + 128, g.dx), col = e0 + 128 - row * g.x;
+    }
+}
+
 // A whole 2D shuffle block [base, base+2048) when every element lies inside x*y and rows
 // are a multiple of 4 elements long (so a group of 4 never straddles a row and halo rows
 // are 16-byte aligned).  Same float expressions as fast2d; the west neighbour's t of lane
 // 0 is carried from lane 31 of the previous group row, row/column advance incrementally,
-// and the next group's loads are issued before the current one is processed.
+// and the loads run two group rows ahead of the arithmetic.  The north row is zero
+// outside the tile, so its prequantised values need no select.
 __device__ __forceinline__ void block2d(const float* __restrict__ in, const Geo& g, uint32_t base, float r,
                                         uint32_t lane, uint32_t* sm, uint32_t& ovf)
 {
-    uint32_t e0  = base + lane * 4;
-    uint32_t row = fdiv(e0, g.dx), col = e0 - row * g.x;
     const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    float4       v  = ldg4(in + e0);
-    float4       u  = (row & 15u) ? ldg4(in + (e0 - g.x)) : z4;
+    uint32_t     e0 = base + lane * 4;
+    uint32_t     row0 = fdiv(e0, g.dx), col0 = e0 - row0 * g.x;
+    uint32_t     row1 = row0, col1 = col0;
+    advance128(g, e0, row1, col1);
+    float4 v0 = ldg4(in + e0), u0 = (row0 & 15u) ? ldg4(in + (e0 - g.x)) : z4;
+    float4 v1 = ldg4(in + e0 + 128), u1 = (row1 & 15u) ? ldg4(in + (e0 + 128 - g.x)) : z4;
     // t = c - n of element base-1, the west neighbour of lane 0's first group
     float carry = 0.0f;
-    if (lane == 0 && (col & 15u))
-        carry = __fsub_rn(pq(__ldg(in + e0 - 1), r), (row & 15u) ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f);
+    if (lane == 0 && (col0 & 15u))
+        carry = __fsub_rn(pq(__ldg(in + e0 - 1), r), (row0 & 15u) ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f);
     bool ov = false;
 #pragma unroll 2
     for (uint32_t it = 0; it < 16; ++it) {
-        const bool rin = (row & 15u) != 0, cin = (col & 15u) != 0;
-        // next group row of this lane: 128 elements on
-        uint32_t rown = row, coln = col + 128;
-        if (g.x >= 128) {
-            if (coln >= g.x) coln -= g.x, ++rown;
-        } else {
-            rown = fdiv(e0 + 128, g.dx), coln = e0 + 128 - rown * g.x;
+        // group row it+2 of this lane: 256 elements on
+        uint32_t row2 = row1, col2 = col1;
+        float4   v2 = z4, u2 = z4;
+        if (it < 14) {
+            advance128(g, e0 + 128, row2, col2);
+            v2 = ldg4(in + e0 + 256);
+            if (row2 & 15u) u2 = ldg4(in + (e0 + 256 - g.x));
         }
-        float4 vn = z4, un = z4;
-        if (it < 15) {
-            vn = ldg4(in + e0 + 128);
-            if (rown & 15u) un = ldg4(in + (e0 + 128 - g.x));
-        }
-        float t[4];
-        t[0] = __fsub_rn(pq(v.x, r), rin ? pq(u.x, r) : 0.0f);
-        t[1] = __fsub_rn(pq(v.y, r), rin ? pq(u.y, r) : 0.0f);
-        t[2] = __fsub_rn(pq(v.z, r), rin ? pq(u.z, r) : 0.0f);
-        t[3] = __fsub_rn(pq(v.w, r), rin ? pq(u.w, r) : 0.0f);
+        const bool cin = (col0 & 15u) != 0;
+        float      t[4];
+        t[0] = __fsub_rn(pq(v0.x, r), pq(u0.x, r));
+        t[1] = __fsub_rn(pq(v0.y, r), pq(u0.y, r));
+        t[2] = __fsub_rn(pq(v0.z, r), pq(u0.z, r));
+        t[3] = __fsub_rn(pq(v0.w, r), pq(u0.w, r));
         const float up = __shfl_up_sync(kFull, t[3], 1);
         const float tw = cin ? (lane ? up : carry) : 0.0f;
         carry          = __shfl_sync(kFull, t[3], 31);
@@ -182,7 +192,9 @@ __device__ __forceinline__ void block2d(const float* __restrict__ in, const Geo&
         }
         const uint32_t q = it * 16 + (lane >> 1);
         *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
-        v = vn, u = un, row = rown, col = coln, e0 += 128;
+        v0 = v1, u0 = u1, row0 = row1, col0 = col1;
+        v1 = v2, u1 = u2, row1 = row2, col1 = col2;
+        e0 += 128;
     }
     ovf |= ov ? 1u : 0u;
 }
@@ -723,7 +735,7 @@ constexpr uint32_t kCompactBlocks = 32;   // shuffle blocks per k_compact CTA
 constexpr uint32_t kSuperBlocks   = 512;  // shuffle blocks per super-tile sum
 
 template <int ND>
-__global__ void __launch_bounds__(kCompressWarps * 32, 3) k_encode(const CompressArgs a, uint4* slots,
+__global__ void __launch_bounds__(kCompressWarps * 32, 4) k_encode(const CompressArgs a, uint4* slots,
                                                                     uint32_t* counts, uint32_t* supers,
                                                                     uint32_t* ovfw)
 {
