@@ -793,13 +793,14 @@ __global__ void __launch_bounds__(256) k_compact(const CompressArgs a, const uin
     __shared__ uint32_t s_red[kCompressWarps], s_tot, s_pre[kCompactBlocks], s_last;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, wid = tid >> 5;
     const uint32_t b0 = blockIdx.x * kCompactBlocks, sup = b0 / kSuperBlocks;
+    // warp 0's own counts are loaded together with everyone's prefix terms
+    const uint32_t c = (wid == 0 && b0 + lane < a.nb) ? __ldcg(counts + b0 + lane) : 0u;
     uint32_t       acc = 0;
     for (uint32_t i = tid; i < sup; i += blockDim.x) acc += __ldcg(supers + i);
     for (uint32_t b = sup * kSuperBlocks + tid; b < b0; b += blockDim.x) acc += __ldcg(counts + b);
     const uint32_t excl = block_sum(acc, s_red);
     if (wid == 0) {
         const uint32_t b = b0 + lane;
-        const uint32_t c = b < a.nb ? __ldcg(counts + b) : 0u;
         uint32_t       v = c;
 #pragma unroll
         for (uint32_t o = 1; o < 32; o <<= 1) {

@@ -195,24 +195,24 @@ __device__ __forceinline__ void decode_group(const DecodeArgs& a, uint32_t g, ui
             bit[q]  = 1u << (8 * q + k);
             lowm[q] = bit[q] - 1u;
         }
-        uint32_t pw  = base;
-        bool     bad = __ldg(a.boff + b + 1) - base !=
-                   (uint32_t)(__popc(b0.x) + __popc(b0.y) + __popc(b0.z) + __popc(b0.w) + __popc(b1.x) +
-                              __popc(b1.y) + __popc(b1.z) + __popc(b1.w));  // table vs bitmap
+        uint32_t       pw  = base;
+        const uint32_t end = __ldg(a.boff + b + 1);
+        // the table agrees with the bitmap and the block's chunks lie inside the stream:
+        // then every rank below is < nnz; otherwise nothing is read
+        const bool bad = end - base != (uint32_t)(__popc(b0.x) + __popc(b0.y) + __popc(b0.z) + __popc(b0.w) +
+                                                  __popc(b1.x) + __popc(b1.y) + __popc(b1.z) + __popc(b1.w)) ||
+                         end < base || end > a.nnz;
+        const uint32_t live = bad ? 0u : kFull;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
+            const uint32_t bmi = bm[i] & live;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int      p    = 4 * i + q;
-                const uint32_t rank = pw + __popc(bm[i] & lowm[q]);
-                uint32_t       v    = 0;
-                if (bm[i] & bit[q]) {
-                    if (rank < a.nnz) v = __ldg(W4 + 4 * (size_t)rank);
-                    else bad = true;
-                }
-                w[p] = v;
+                const uint32_t rank = pw + __popc(bmi & lowm[q]);
+                w[p]                = (bmi & bit[q]) ? __ldg(W4 + 4 * (size_t)rank) : 0u;
             }
-            pw += __popc(bm[i]);
+            pw += __popc(bmi);
         }
         if (bad) atomicOr(a.status, kStatusCorrupt);
         transpose32(w);  // w[p] = S[p*32 + gg]  ->  w[j] = W[gg*32 + j]
