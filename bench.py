@@ -38,9 +38,15 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-DIMS = (39200, 388, 1)
-EB = 1e-3
-WORKLOAD = "exafel-like 39200x388 f32 (peaks on N(0,0.5) background), relative eb 1e-3"
+# single-field workloads (--field): dims, relative eb, generator, description.  The
+# headline is exafel (the workload the metric is quoted on); the others profile the
+# other dimensionalities on the same harness.
+FIELDS = {
+    "exafel": ((39200, 388, 1), 1e-3, "peaks2d", "exafel-like 39200x388 f32 (peaks on N(0,0.5) background), relative eb 1e-3"),
+    "cesm": ((3600, 1800, 1), 1e-3, "smooth2d", "cesm-like 3600x1800 f32 (smooth, ~30% zeros), relative eb 1e-3"),
+    "hurricane": ((500, 500, 100), 1e-3, "smooth3d", "hurricane-like 500x500x100 f32 (smooth 3D, ~40% zeros), relative eb 1e-3"),
+}
+DIMS, EB, KIND, WORKLOAD = FIELDS["exafel"]
 METRIC = "compress/decompress GB/s + %HBM peak"
 
 
@@ -54,7 +60,10 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--workload", choices=["exafel", "batch", "serving"], default="exafel",
-                   help="exafel: the headline line; batch: configs[3]; serving: configs[4]")
+                   help="exafel: the headline line (single-field workload, see --field); batch: configs[3]; "
+                        "serving: configs[4]")
+    p.add_argument("--field", choices=sorted(FIELDS), default="exafel",
+                   help="the single-field workload of the headline line (default exafel)")
     p.add_argument("--batch-fields", type=int, default=512)
     p.add_argument("--serve-seconds", type=float, default=3.0)
     p.add_argument("--serve-rate", type=float, default=2000.0)
@@ -156,7 +165,7 @@ def make_fields(count, seed0):
     import __graft_entry__ as g
     g.load_package()
     synth = importlib.import_module("fz_gpu_gb300.synth")
-    return [synth.peaks2d(DIMS[0], DIMS[1], seed=seed0 + i) for i in range(count)]
+    return [synth.field(KIND, DIMS, seed0 + i) for i in range(count)]
 
 
 def cpu_round_trips(field, seconds, min_reps=2):
@@ -198,7 +207,7 @@ def run_reference(args, rank, world):
         "config": {"workload": WORKLOAD + ", one field per step (compress + decompress)",
                    "field_elems": n},
         "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": oracle.threads(), "kind": "port",
-                         "sample": f"{args.steps} round trips of one {DIMS[0]}x{DIMS[1]} field"},
+                         "sample": f"{args.steps} round trips of one {'x'.join(map(str, DIMS))} field"},
         "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -362,7 +371,7 @@ def run_fz(args, rank, world, local_rank):
         oracle.build()
         gbs, reps, el = cpu_round_trips(fields[0], args.cpu_seconds)
         line["cpu_baseline"] = {"value": round(gbs, 3), "unit": "GB/s", "cores": oracle.threads(),
-                                "kind": "port", "sample": f"{reps} round trips of one {DIMS[0]}x{DIMS[1]} field ({el:.1f} s)"}
+                                "kind": "port", "sample": f"{reps} round trips of one {'x'.join(map(str, DIMS))} field ({el:.1f} s)"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -645,7 +654,9 @@ def run_serving(args, local_rank):
 
 
 def main():
+    global DIMS, EB, KIND, WORKLOAD
     args = parse_args()
+    DIMS, EB, KIND, WORKLOAD = FIELDS[args.field]
     rank, world, local_rank = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -345,3 +345,18 @@ def test_batch_branch_counts_and_autotune(fz, oracle, synth):
     with pytest.raises(fz.FzError):
         fz.Batch(ws, comp, fz.COMPRESS, branches=17)
     assert ws.status() == fz.SUCCESS
+
+
+@pytest.mark.parametrize("nblocks,extra", [(512, 0), (1024, 0), (1025, 5), (31, 2047), (32, 0), (33, 1), (544, 100)])
+def test_compaction_group_boundaries(fz, oracle, ws, nblocks, extra):
+    """Fields ending exactly on or just past a 512-block count group and a 32-block
+    compaction CTA: offsets, offset table and header match the oracle."""
+    n = nblocks * 2048 + extra
+    rng = np.random.default_rng(n)
+    data = np.cumsum(rng.normal(0, 1, n)).astype(np.float32)
+    data[rng.random(n) < 0.3] = 0  # uneven chunk counts per block
+    for mode in (0, 1):
+        st, got, want = run_both(fz, oracle, ws, data, (n, 1, 1), 1e-3, mode=mode)
+        assert_same_stream(got, want)
+        rec = fz.decompress(st, ws=ws).cpu().numpy()
+        assert np.array_equal(rec.view(np.uint32), oracle.decompress(want).view(np.uint32))
