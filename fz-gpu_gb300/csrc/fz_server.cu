@@ -9,15 +9,23 @@
 // Requests wait in a FIFO.  Host-buffer requests (pinned ones let the copies overlap)
 // are staged through pool buffers; device-resident requests (FZ_REQUEST_DEVICE) run on
 // the caller's device buffers and only count their bytes against the pool.
-// fz_server_poll never blocks: it retires requests whose work has finished, then admits
-// queued requests while a slot is free and the pool can hold their buffers.  Requests
-// on different slots overlap on the device (copies on the copy engines, kernels
-// side by side), so work that arrives while others run starts as soon as memory and a
-// slot free up.
+// Worker threads (up to kWorkers, each owning every kWorkers-th slot) retire requests
+// whose work has finished and admit queued requests while a slot is free and the pool
+// can hold their buffers; the CUDA calls that issue a request (launches, copies) run
+// outside the server's lock, so several requests are issued at once.
+// fz_server_poll never blocks: it hands out the completions.  Requests on different
+// slots overlap on the device (copies on the copy engines, kernels side by side), so
+// work that arrives while others run starts as soon as memory and a slot free up.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
 #include <cstring>
 #include <deque>
 #include <map>
+#include <mutex>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "../../include/fz.h"
@@ -103,13 +111,23 @@ struct Queued {
     bool       has_header;
 };
 
+constexpr uint32_t kWorkers = 8;  // issuing threads (at most one per slot)
+
 struct fz_server {
     uint8_t*                   d_pool = nullptr;
     Pool*                      pool   = nullptr;
     uint64_t                   budget = 0, max_n = 0;
-    std::vector<Slot>          slots;
+    int                        device = 0;
+    std::vector<Slot>          slots;  // slot i belongs to worker i % workers.size()
+    // guarded by mu: queue, done, pool, running
+    std::mutex                 mu;
+    std::condition_variable    cv;     // new requests, shutdown
     std::deque<Queued>         queue;
-    std::deque<fz_completion>  done;  // finished but not yet handed out
+    std::deque<fz_completion>  done;   // finished but not yet handed out
+    std::atomic<uint32_t>      ndone{0};  // done.size(), read without the lock by poll
+    uint32_t                   running = 0;
+    std::atomic<bool>          stop{false};
+    std::vector<std::thread>   workers;
 };
 
 namespace {
@@ -136,11 +154,16 @@ bool request_bytes(const fz_request& r, uint64_t* src, uint64_t* dst)
     return true;
 }
 
+// Hands a slot's request back (pool bytes released, completion queued).  Called by the
+// slot's worker.
 void finish(fz_server* S, Slot& sl, fz_status st, uint64_t result)
 {
+    std::lock_guard<std::mutex> lk(S->mu);
     S->pool->release(sl.src_off, sl.src_bytes);
     S->pool->release(sl.dst_off, sl.dst_bytes);
     S->done.push_back(fz_completion{sl.req.id, st, result});
+    S->ndone.store((uint32_t)S->done.size(), std::memory_order_release);
+    --S->running;
     sl.phase = Phase::Idle;
 }
 
@@ -215,7 +238,122 @@ fz_status status_word(const Slot& sl)
     return FZ_SUCCESS;
 }
 
+// A busy slot whose current phase has finished moves on: a device stream's header has
+// arrived (issue its decompression), a compressed stream's header has arrived (copy the
+// stream home, or finish a device request), or the request is done.  Returns true when
+// the slot changed state.
+bool retire(fz_server* S, Slot& sl)
+{
+    const cudaError_t q = cudaEventQuery(sl.ev);
+    if (q == cudaErrorNotReady) return false;
+    if (q != cudaSuccess) {
+        finish(S, sl, FZ_FAIL_GPU_ILLEGAL_ACCESS, 0);
+        return true;
+    }
+    if (sl.phase == Phase::WaitInHeader) {
+        fz_header h;
+        std::memcpy(&h, sl.h_buf, sizeof(h));
+        const fz_status st = issue_decompress(S, sl, h);
+        if (st != FZ_SUCCESS) {
+            cudaStreamSynchronize(sl.stream);
+            finish(S, sl, st, 0);
+        }
+        return true;
+    }
+    if (sl.phase == Phase::WaitHeader) {
+        fz_header h;
+        std::memcpy(&h, sl.h_buf, sizeof(h));
+        uint64_t  bytes = 0;
+        fz_status st    = status_word(sl);
+        if (st == FZ_SUCCESS) st = fz_stream_bytes(&h, &bytes);
+        if (st == FZ_SUCCESS && bytes > sl.req.dst_capacity) st = FZ_OUT_OF_SPACE;
+        if (st != FZ_SUCCESS || is_device(sl.req)) {  // a device result is in place already
+            finish(S, sl, st, st == FZ_SUCCESS ? bytes : 0);
+            return true;
+        }
+        if (cudaMemcpyAsync(sl.req.dst, S->d_pool + sl.dst_off, bytes, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+            st = FZ_FAIL_GPU_MEMCPY;
+        if (st == FZ_SUCCESS && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
+        if (st != FZ_SUCCESS) {
+            finish(S, sl, st, 0);
+            return true;
+        }
+        sl.result = bytes;
+        sl.phase  = Phase::WaitDone;
+        return true;
+    }
+    finish(S, sl, sl.req.dir == FZ_DECOMPRESS ? status_word(sl) : FZ_SUCCESS, sl.result);
+    return true;
+}
+
+// Admits the head of the queue onto an idle slot if the pool can hold it (first come,
+// first served; requests that can never run complete at once with an error).  The
+// request is issued outside the lock.  Returns true when something was admitted or
+// rejected.
+bool admit(fz_server* S, Slot& sl)
+{
+    fz_request r;
+    uint64_t   so = 0, sb = 0, dof = 0, db = 0;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        bool                        changed = false;
+        for (;;) {
+            if (S->queue.empty()) return changed;
+            const Queued& qf = S->queue.front();
+            r                = qf.r;
+            // a device-resident stream's element count is only known once its header is read
+            // (fz_decompress checks it against the slot's workspace and dst_capacity then)
+            const bool     dev_dec   = r.dir == FZ_DECOMPRESS && is_device(r);
+            const uint64_t n         = r.dir == FZ_COMPRESS ? r.n
+                                       : dev_dec            ? 0
+                                                            : reinterpret_cast<const fz_header*>(r.src)->n;
+            const bool     small_dst = r.dir == FZ_DECOMPRESS && 4 * n > r.dst_capacity;
+            if (!request_bytes(r, &sb, &db) || n > S->max_n || small_dst || sb + db + 512 > S->budget) {
+                S->done.push_back(fz_completion{r.id, n > S->max_n ? FZ_INVALID_ARG : FZ_OUT_OF_SPACE, 0});
+                S->ndone.store((uint32_t)S->done.size(), std::memory_order_release);
+                S->queue.pop_front();  // can never run
+                changed = true;
+                continue;
+            }
+            if (!S->pool->alloc(sb, &so)) return changed;  // wait for memory to free up
+            if (!S->pool->alloc(db, &dof)) {
+                S->pool->release(so, sb);
+                return changed;
+            }
+            sl.hdr = qf.h;
+            if (qf.has_header) r.header = &sl.hdr;
+            S->queue.pop_front();
+            ++S->running;
+            break;
+        }
+    }
+    issue(S, sl, r, so, sb, dof, db);
+    return true;
+}
+
+void worker(fz_server* S, uint32_t first, uint32_t stride)
+{
+    cudaSetDevice(S->device);
+    while (!S->stop.load(std::memory_order_relaxed)) {
+        bool progress = false, busy = false;
+        for (uint32_t i = first; i < S->slots.size(); i += stride) {
+            Slot& sl = S->slots[i];
+            if (sl.phase != Phase::Idle) progress |= retire(S, sl);
+            if (sl.phase == Phase::Idle) progress |= admit(S, sl);
+            busy |= sl.phase != Phase::Idle;
+        }
+        if (progress) continue;
+        if (busy) {
+            std::this_thread::yield();  // work in flight: look again soon
+        } else {
+            std::unique_lock<std::mutex> lk(S->mu);
+            S->cv.wait_for(lk, std::chrono::milliseconds(1), [S] { return !S->queue.empty() || S->stop.load(); });
+        }
+    }
+}
+
 }  // namespace
+
 
 extern "C" {
 
@@ -231,6 +369,7 @@ fz_status fz_server_create(uint64_t hbm_budget, uint32_t slots, uint64_t max_n, 
         return FZ_FAIL_GPU_OUT_OF_MEMORY;
     }
     S->pool = new Pool(hbm_budget);
+    cudaGetDevice(&S->device);
     S->slots.resize(slots);
     for (Slot& sl : S->slots) {
         fz_status st = fz_workspace_create(max_n, &sl.ws);
@@ -244,6 +383,8 @@ fz_status fz_server_create(uint64_t hbm_budget, uint32_t slots, uint64_t max_n, 
             return st;
         }
     }
+    const uint32_t nw = std::min(kWorkers, slots);
+    for (uint32_t k = 0; k < nw; ++k) S->workers.emplace_back(worker, S, k, nw);
     *out = S;
     return FZ_SUCCESS;
 }
@@ -256,94 +397,26 @@ fz_status fz_server_submit(fz_server* S, const fz_request* r)
     Queued q{*r, {}, r->header != nullptr};
     if (q.has_header) q.h = *r->header;
     q.r.header = nullptr;  // re-pointed at the slot's copy when the request is issued
-    S->queue.push_back(q);
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->queue.push_back(q);
+    }
+    S->cv.notify_one();
     return FZ_SUCCESS;
 }
 
 fz_status fz_server_poll(fz_server* S, fz_completion* out, uint32_t max, uint32_t* count)
 {
     if (!S || !count || (!out && max)) return FZ_INVALID_ARG;
-    // retire
-    for (Slot& sl : S->slots) {
-        if (sl.phase == Phase::Idle) continue;
-        const cudaError_t q = cudaEventQuery(sl.ev);
-        if (q == cudaErrorNotReady) continue;
-        if (q != cudaSuccess) {
-            finish(S, sl, FZ_FAIL_GPU_ILLEGAL_ACCESS, 0);
-            continue;
-        }
-        if (sl.phase == Phase::WaitInHeader) {
-            fz_header h;
-            std::memcpy(&h, sl.h_buf, sizeof(h));
-            const fz_status st = issue_decompress(S, sl, h);
-            if (st != FZ_SUCCESS) {
-                cudaStreamSynchronize(sl.stream);
-                finish(S, sl, st, 0);
-            }
-            continue;
-        }
-        if (sl.phase == Phase::WaitHeader) {
-            fz_header h;
-            std::memcpy(&h, sl.h_buf, sizeof(h));
-            uint64_t  bytes = 0;
-            fz_status st    = status_word(sl);
-            if (st == FZ_SUCCESS) st = fz_stream_bytes(&h, &bytes);
-            if (st == FZ_SUCCESS && bytes > sl.req.dst_capacity) st = FZ_OUT_OF_SPACE;
-            if (st != FZ_SUCCESS || is_device(sl.req)) {  // a device result is in place already
-                finish(S, sl, st, st == FZ_SUCCESS ? bytes : 0);
-                continue;
-            }
-            if (cudaMemcpyAsync(sl.req.dst, S->d_pool + sl.dst_off, bytes, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
-                st = FZ_FAIL_GPU_MEMCPY;
-            if (st == FZ_SUCCESS && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
-            if (st != FZ_SUCCESS) {
-                finish(S, sl, st, 0);
-                continue;
-            }
-            sl.result = bytes;
-            sl.phase  = Phase::WaitDone;
-            continue;
-        }
-        finish(S, sl, sl.req.dir == FZ_DECOMPRESS ? status_word(sl) : FZ_SUCCESS, sl.result);
-    }
-    // admit, first come first served
-    while (!S->queue.empty()) {
-        Slot* free_slot = nullptr;
-        for (Slot& sl : S->slots)
-            if (sl.phase == Phase::Idle) {
-                free_slot = &sl;
-                break;
-            }
-        if (!free_slot) break;
-        const Queued     qf = S->queue.front();
-        fz_request       r  = qf.r;
-        uint64_t         sb = 0, db = 0;
-        // a device-resident stream's element count is only known once its header is read
-        // (fz_decompress checks it against the slot's workspace and dst_capacity then)
-        const bool     dev_dec = r.dir == FZ_DECOMPRESS && is_device(r);
-        const uint64_t n = r.dir == FZ_COMPRESS ? r.n : dev_dec ? 0 : reinterpret_cast<const fz_header*>(r.src)->n;
-        const bool small_dst = r.dir == FZ_DECOMPRESS && 4 * n > r.dst_capacity;
-        if (!request_bytes(r, &sb, &db) || n > S->max_n || small_dst || sb + db + 512 > S->budget) {
-            S->queue.pop_front();  // can never run
-            S->done.push_back(fz_completion{r.id, n > S->max_n ? FZ_INVALID_ARG : FZ_OUT_OF_SPACE, 0});
-            continue;
-        }
-        uint64_t so = 0, dof = 0;
-        if (!S->pool->alloc(sb, &so)) break;  // wait for memory to free up
-        if (!S->pool->alloc(db, &dof)) {
-            S->pool->release(so, sb);
-            break;
-        }
-        S->queue.pop_front();
-        free_slot->hdr = qf.h;
-        if (qf.has_header) r.header = &free_slot->hdr;
-        issue(S, *free_slot, r, so, sb, dof, db);
-    }
-    uint32_t k = 0;
+    *count = 0;
+    if (S->ndone.load(std::memory_order_acquire) == 0) return FZ_SUCCESS;  // nothing to hand out: no lock
+    std::lock_guard<std::mutex> lk(S->mu);
+    uint32_t                    k = 0;
     while (k < max && !S->done.empty()) {
         out[k++] = S->done.front();
         S->done.pop_front();
     }
+    S->ndone.store((uint32_t)S->done.size(), std::memory_order_release);
     *count = k;
     return FZ_SUCCESS;
 }
@@ -351,10 +424,9 @@ fz_status fz_server_poll(fz_server* S, fz_completion* out, uint32_t max, uint32_
 fz_status fz_server_pending(fz_server* S, uint32_t* queued, uint32_t* running, uint64_t* pool_used)
 {
     if (!S) return FZ_INVALID_ARG;
-    uint32_t r = 0;
-    for (const Slot& sl : S->slots) r += sl.phase != Phase::Idle;
+    std::lock_guard<std::mutex> lk(S->mu);
     if (queued) *queued = (uint32_t)S->queue.size();
-    if (running) *running = r;
+    if (running) *running = S->running;
     if (pool_used) *pool_used = S->pool->used();
     return FZ_SUCCESS;
 }
@@ -362,6 +434,9 @@ fz_status fz_server_pending(fz_server* S, uint32_t* queued, uint32_t* running, u
 fz_status fz_server_destroy(fz_server* S)
 {
     if (!S) return FZ_INVALID_ARG;
+    S->stop.store(true);
+    S->cv.notify_all();
+    for (std::thread& t : S->workers) t.join();
     for (Slot& sl : S->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         if (sl.ws) fz_workspace_destroy(sl.ws);

@@ -332,9 +332,11 @@ typedef struct fz_completion {
    its own workspace, share one device pool of hbm_budget bytes from which every admitted
    host-buffer request takes its input and output buffers (a device-resident request
    counts its input and output bytes against the same budget).  Requests queue in arrival order;
-   fz_server_poll (non-blocking) retires finished requests and admits queued ones as
-   slots and pool memory free up, so requests that arrive while others run overlap on
-   the device.  No counterpart in the reference (one field per process, fz.cu:226-238). */
+   the server's worker threads (up to 8, each owning some slots) retire finished requests
+   and admit queued ones as slots and pool memory free up, so requests that arrive while
+   others run overlap on the device; fz_server_poll (non-blocking) hands out the
+   completions.  The functions may be called from any thread.  No counterpart in the
+   reference (one field per process, fz.cu:226-238). */
 typedef struct fz_server fz_server;
 fz_status fz_server_create(uint64_t hbm_budget, uint32_t slots, uint64_t max_n, fz_server** out);
 fz_status fz_server_submit(fz_server* server, const fz_request* request);
