@@ -342,6 +342,17 @@ fz_status fz_compress(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims d
                       fz_eb_mode eb_mode, fz_mode mode, void* d_out, uint64_t out_capacity,
                       uint64_t* out_bytes, fz_stream_t stream)
 {
+    return fz::compress_impl(ws, d_in, n, dims, eb, eb_mode, mode, d_out, out_capacity, out_bytes, stream, nullptr);
+}
+
+}  // extern "C"
+
+// fz_compress with an optional device mirror of the header and status word (128 bytes,
+// written by the last kernel; the request loop reads both with one copy).
+fz_status fz::compress_impl(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims dims, double eb,
+                            fz_eb_mode eb_mode, fz_mode mode, void* d_out, uint64_t out_capacity,
+                            uint64_t* out_bytes, fz_stream_t stream, uint32_t* mirror)
+{
     if (!ws || !d_in || !d_out || !aligned16(d_in) || !aligned16(d_out)) return FZ_INVALID_ARG;
     if (check_dims(n, dims) != FZ_SUCCESS || n > ws->max_n) return FZ_INVALID_ARG;
     if (!(eb > 0) || !std::isfinite(eb)) return FZ_INVALID_ARG;
@@ -363,6 +374,7 @@ fz_status fz_compress(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims d
     a.off_a = L.off_a, a.off_c = L.off_c, a.off_b = L.off_b, a.off_sign = L.off_sign, a.off_boff = L.off_boff;
     a.state = ws->state, a.ticket = ws->tickets + 0, a.status = ws->status, a.epoch = ws->epoch;
     a.boff  = mode == FZ_MODE_SIDECAR ? reinterpret_cast<uint32_t*>(a.out + L.off_boff) : nullptr;
+    a.mirror = mirror;
     cudaError_t e = cudaSuccess;
     if (eb_mode == FZ_EB_REL) {
         KernelTimer t(ws, s, 0);
@@ -396,6 +408,8 @@ fz_status fz_compress(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims d
     }
     return FZ_SUCCESS;
 }
+
+extern "C" {
 
 fz_status fz_decompress(fz_workspace* ws, const void* d_stream, uint64_t stream_bytes,
                         const fz_header* h_header, float* d_out, uint64_t out_capacity_elems,

@@ -858,6 +858,15 @@ __global__ void __launch_bounds__(256) k_compact(const CompressArgs a, const uin
         *ovfw = 0;
         *done = 0;
         if (a.mm) a.mm[0] = 0xFFFFFFFFu, a.mm[1] = 0u;  // empty range for the next call
+        if (a.mirror) {
+            // header and status in one place, so a caller reads both with one copy
+            __threadfence();
+            const uint4* h = reinterpret_cast<const uint4*>(a.out);
+            uint4*       m = reinterpret_cast<uint4*>(a.mirror);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) m[i] = __ldcg(h + i);
+            a.mirror[16] = __ldcg(a.status);
+        }
     }
 }
 

@@ -40,6 +40,7 @@ struct CompressArgs {
     uint32_t*    status;
     uint32_t*    epoch;  // device epoch word (advanced by the kernel's last ticket fetch)
     uint32_t*    boff;   // block offset table in the stream's sidecar, or null
+    uint32_t*    mirror; // k_compact: 64-byte header + status word copied here, or null
 };
 
 struct DecodeArgs {

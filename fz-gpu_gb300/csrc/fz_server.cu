@@ -87,6 +87,7 @@ struct Slot {
     cudaStream_t  stream = nullptr;
     fz_workspace* ws     = nullptr;
     uint8_t*      h_buf  = nullptr;  // pinned: header (64 B) + status word
+    uint32_t*     d_mirror = nullptr;  // device: header + status of a compression (one copy home)
     cudaEvent_t   ev     = nullptr;
     Phase         phase  = Phase::Idle;
     fz_request    req{};
@@ -201,12 +202,11 @@ void issue(fz_server* S, Slot& sl, const fz_request& r, uint64_t src_off, uint64
         st = FZ_FAIL_GPU_MEMCPY;
     if (r.dir == FZ_COMPRESS) {
         if (st == FZ_SUCCESS)
-            st = fz_compress(sl.ws, reinterpret_cast<const float*>(d_src), r.n, r.dims, r.eb, r.eb_mode, r.mode,
-                             d_dst, dev ? r.dst_capacity : dst_b, nullptr, hs);
-        // header and status come back first; the stream's length follows from nnz
-        if (st == FZ_SUCCESS && cudaMemcpyAsync(sl.h_buf, d_dst, 64, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
-            st = FZ_FAIL_GPU_MEMCPY;
-        if (st == FZ_SUCCESS && cudaMemcpyAsync(sl.h_buf + 64, sl.ws->status, 4, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+            st = compress_impl(sl.ws, reinterpret_cast<const float*>(d_src), r.n, r.dims, r.eb, r.eb_mode, r.mode,
+                               d_dst, dev ? r.dst_capacity : dst_b, nullptr, hs, sl.d_mirror);
+        // header and status come back first, in one copy of the mirror; the stream's
+        // length follows from nnz
+        if (st == FZ_SUCCESS && cudaMemcpyAsync(sl.h_buf, sl.d_mirror, 68, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
             st = FZ_FAIL_GPU_MEMCPY;
         if (st == FZ_SUCCESS && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
         sl.phase = Phase::WaitHeader;
@@ -228,10 +228,16 @@ void issue(fz_server* S, Slot& sl, const fz_request& r, uint64_t src_off, uint64
     }
 }
 
+// The request's status from the word copied home; a set word is cleared on the device
+// (it is sticky in the workspace) so the slot's next request starts clean.
 fz_status status_word(const Slot& sl)
 {
     uint32_t w;
     std::memcpy(&w, sl.h_buf + 64, 4);
+    if (w) {
+        cudaMemsetAsync(sl.ws->status, 0, 4, sl.stream);
+        cudaStreamSynchronize(sl.stream);
+    }
     if (w & kStatusTimeout) return FZ_TIMEOUT;
     if (w & kStatusNonfinite) return FZ_NONFINITE_INPUT;
     if (w & kStatusCorrupt) return FZ_CORRUPT_STREAM;
@@ -376,6 +382,7 @@ fz_status fz_server_create(uint64_t hbm_budget, uint32_t slots, uint64_t max_n, 
         if (st == FZ_SUCCESS && cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess)
             st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
         if (st == FZ_SUCCESS && cudaMallocHost((void**)&sl.h_buf, 128) != cudaSuccess) st = FZ_FAIL_GPU_MALLOC;
+        if (st == FZ_SUCCESS && cudaMalloc((void**)&sl.d_mirror, 128) != cudaSuccess) st = FZ_FAIL_GPU_MALLOC;
         if (st == FZ_SUCCESS && cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess)
             st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
         if (st != FZ_SUCCESS) {
@@ -442,6 +449,7 @@ fz_status fz_server_destroy(fz_server* S)
         if (sl.ws) fz_workspace_destroy(sl.ws);
         if (sl.stream) cudaStreamDestroy(sl.stream);
         if (sl.h_buf) cudaFreeHost(sl.h_buf);
+        if (sl.d_mirror) cudaFree(sl.d_mirror);
         if (sl.ev) cudaEventDestroy(sl.ev);
     }
     cudaFree(S->d_pool);

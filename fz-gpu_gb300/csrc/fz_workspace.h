@@ -3,6 +3,7 @@
 
 #include <vector>
 
+#include "../../include/fz.h"
 #include "fz_internal.h"
 
 struct fz_workspace {
@@ -34,3 +35,10 @@ struct fz_workspace {
     uint32_t                 tused = 0;
 };
 
+namespace fz {
+// fz_compress with an optional device mirror (128 bytes, 16-byte aligned) that receives
+// the 64-byte header and, at word 16, the status word once the stream is complete.
+fz_status compress_impl(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims dims, double eb,
+                        fz_eb_mode eb_mode, fz_mode mode, void* d_out, uint64_t out_capacity,
+                        uint64_t* out_bytes, fz_stream_t stream, uint32_t* mirror);
+}  // namespace fz

@@ -125,3 +125,26 @@ def test_device_request_with_short_output_fails_cleanly(fz, synth):
     assert done[1][0] == fz.OUT_OF_SPACE
     assert server.pending() == (0, 0, 0)
     server.close()
+
+
+def test_failed_request_does_not_poison_its_slot(fz, synth):
+    """A request that fails on the device (non-finite input with a relative eb) reports
+    FZ_NONFINITE_INPUT; the same slot then serves the next request normally."""
+    good = synth.smooth2d(300, 200, seed=49)
+    bad = good.copy()
+    bad[123] = np.nan
+    ws = fz.Workspace(good.size)
+    alone = fz.compress(torch.from_numpy(good).cuda(), (300, 200, 1), 1e-3, ws=ws).cpu().numpy()
+    xb, xg = torch.from_numpy(bad).cuda(), torch.from_numpy(good).cuda()
+    cap = fz.max_compressed_bytes(good.size, (300, 200, 1))
+    outs = [torch.zeros(cap, dtype=torch.uint8, device="cuda") for _ in range(2)]
+    server = fz.Server(64 << 20, 1, good.size)
+    for rid, (x, o) in enumerate(((xb, outs[0]), (xg, outs[1]))):
+        done = _run(fz, server, [dict(rid=rid, direction=fz.COMPRESS, src=x.data_ptr(), dst=o.data_ptr(),
+                                      dst_capacity=cap, n=good.size, dims=(300, 200, 1), eb=1e-3, device=True)])
+        if rid == 0:
+            assert done[0][0] == fz.NONFINITE_INPUT
+        else:
+            assert done[1][0] == fz.SUCCESS and done[1][1] == alone.size
+            assert np.array_equal(outs[1][: alone.size].cpu().numpy(), alone)
+    server.close()
