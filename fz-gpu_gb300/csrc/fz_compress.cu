@@ -163,7 +163,7 @@ __device__ __forceinline__ void block2d(const float* __restrict__ in, const Geo&
     float carry = 0.0f;
     if (lane == 0 && (col0 & 15u))
         carry = __fsub_rn(pq(__ldg(in + e0 - 1), r), (row0 & 15u) ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f);
-    bool ov = false;
+    float amax = 0.0f;  // max |d| (NaN if any d is NaN)
 #pragma unroll 2
     for (uint32_t it = 0; it < 16; ++it) {
         // group row it+2 of this lane: 256 elements on
@@ -183,20 +183,20 @@ __device__ __forceinline__ void block2d(const float* __restrict__ in, const Geo&
         const float up = __shfl_up_sync(kFull, t[3], 1);
         const float tw = cin ? (lane ? up : carry) : 0.0f;
         carry          = __shfl_sync(kFull, t[3], 31);
-        uint32_t c[4];
+        float d[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float d = __fsub_rn(t[j], j ? t[j - 1] : tw);
-            c[j]          = pack_signed(d);
-            ov |= !(fabsf(d) < 32768.0f);
+            d[j] = __fsub_rn(t[j], j ? t[j - 1] : tw);
+            amax = fmax_nan(amax, fabsf(d[j]));
         }
         const uint32_t q = it * 16 + (lane >> 1);
-        *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+        *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
+            make_uint2(pack_signed_pair(d[0], d[1]), pack_signed_pair(d[2], d[3]));
         v0 = v1, u0 = u1, row0 = row1, col0 = col1;
         v1 = v2, u1 = u2, row1 = row2, col1 = col2;
         e0 += 128;
     }
-    ovf |= ov ? 1u : 0u;
+    ovf |= !(amax < 32768.0f) ? 1u : 0u;
 }
 
 // Plane/row/column of element e0 + 128 given that of e0 (x a multiple of 4).
@@ -243,7 +243,7 @@ __device__ __forceinline__ void block3d(const float* __restrict__ in, const Geo&
         bw  = zi ? pq(__ldg(in + e0 - 1 - g.xy), r) : 0.0f;
         bnw = (zi && yi) ? pq(__ldg(in + e0 - 1 - g.xy - g.x), r) : 0.0f;
     }
-    bool ov = false;
+    float amax = 0.0f;  // max |d| (NaN if any d is NaN)
 #pragma unroll 1
     for (uint32_t it = 0; it < 16; ++it) {
         uint32_t zn = zz, yn = yy, xn = xx;
@@ -269,7 +269,7 @@ __device__ __forceinline__ void block3d(const float* __restrict__ in, const Geo&
         bw  = __shfl_sync(kFull, bq[3], 31);
         bnw = __shfl_sync(kFull, bn[3], 31);
         if ((xx & 7u) == 0) wp = wn = wb = wbn = 0.0f;  // the group starts a tile row
-        uint32_t c[4];
+        float d[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             // c - (A - B - C - D + E + F + G), lorenzo_var.cuh:277-283; absent terms are 0
@@ -279,16 +279,16 @@ __device__ __forceinline__ void block3d(const float* __restrict__ in, const Geo&
             s       = __fadd_rn(s, j ? p[j - 1] : wp);
             s       = __fadd_rn(s, nq[j]);
             s       = __fadd_rn(s, bq[j]);
-            const float d = __fsub_rn(p[j], s);
-            c[j]          = pack_signed(d);
-            ov |= !(fabsf(d) < 32768.0f);
+            d[j]    = __fsub_rn(p[j], s);
+            amax    = fmax_nan(amax, fabsf(d[j]));
         }
         const uint32_t q = it * 16 + (lane >> 1);
-        *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+        *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
+            make_uint2(pack_signed_pair(d[0], d[1]), pack_signed_pair(d[2], d[3]));
         v = vn, un = unn, ub = ubn, uc = ucn, zz = zn, yy = yn, xx = xn;
         e0 += 128;
     }
-    ovf |= ov ? 1u : 0u;
+    ovf |= !(amax < 32768.0f) ? 1u : 0u;
 }
 
 template <int ND>

@@ -81,6 +81,23 @@ __device__ __forceinline__ uint32_t pack_signed(float d)
     tmp |= ((d < 0) << 15);
     return tmp;
 }
+// Two sign-magnitude codes in one word: pack_signed(d0) | pack_signed(d1) << 16.  The
+// (uint16_t) conversion of lorenzo_var.cuh:169-171 is a saturating f32 -> u32 conversion
+// whose low 16 bits are kept; one byte permute takes both low halves, then both signs
+// (d < 0: false for -0 and NaN) are OR-ed in.
+__device__ __forceinline__ uint32_t pack_signed_pair(float d0, float d1)
+{
+    const uint32_t m0 = static_cast<uint32_t>(fabsf(d0)), m1 = static_cast<uint32_t>(fabsf(d1));
+    return __byte_perm(m0, m1, 0x5410) | (d0 < 0.0f ? 0x8000u : 0u) | (d1 < 0.0f ? 0x80000000u : 0u);
+}
+// max(a, b) that returns NaN when either is NaN (max.NaN.f32): a running max of |d|
+// answers "some delta does not fit 15 bits, or is NaN" with one compare at the end.
+__device__ __forceinline__ float fmax_nan(float a, float b)
+{
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
 // 1D positions i%4 != 0 store the magnitude only (lorenzo_var.cuh:62).
 __device__ __forceinline__ uint32_t pack_unsigned(float d)
 {
