@@ -199,6 +199,51 @@ __device__ __forceinline__ void block2d(const float* __restrict__ in, const Geo&
     ovf |= !(amax < 32768.0f) ? 1u : 0u;
 }
 
+// A whole 1D shuffle block [base, base+2048) inside the field (c_lorenzo_1d1l,
+// lorenzo_var.cuh:176-214): 256-element Lorenzo blocks with p[-1] = 0 at their start;
+// the code at i%4 == 0 carries its sign, the others the magnitude only (Q2), and the
+// signs of all deltas go to the sidecar words when signw is set.  Lane 0's west
+// neighbour is carried from lane 31 of the previous group row (group rows at odd
+// multiples of 128 continue a 256-element block), and the next row's load is issued
+// before the current one is processed.
+__device__ __forceinline__ void block1d(const float* __restrict__ in, uint32_t base, float r, uint32_t lane,
+                                        uint32_t* sm, uint32_t* signw, uint32_t& ovf)
+{
+    uint32_t e0    = base + lane * 4;
+    float4   v     = ldg4(in + e0);
+    float    carry = 0.0f;
+    float    amax0 = 0.0f, amax1 = 0.0f;  // max |d| of the signed / magnitude-only positions
+#pragma unroll 2
+    for (uint32_t it = 0; it < 16; ++it) {
+        const float4 vn = it < 15 ? ldg4(in + e0 + 128) : v;
+        const float  p0 = pq(v.x, r), p1 = pq(v.y, r), p2 = pq(v.z, r), p3 = pq(v.w, r);
+        const float  up = __shfl_up_sync(kFull, p3, 1);
+        const float  w  = (e0 & 255u) ? (lane ? up : carry) : 0.0f;
+        carry           = __shfl_sync(kFull, p3, 31);
+        const float d0 = __fsub_rn(p0, w), d1 = __fsub_rn(p1, p0), d2 = __fsub_rn(p2, p1), d3 = __fsub_rn(p3, p2);
+        amax0          = fmax_nan(amax0, fabsf(d0));
+        amax1          = fmax_nan(amax1, fmax_nan(fabsf(d1), fmax_nan(fabsf(d2), fabsf(d3))));
+        const uint32_t m0 = static_cast<uint32_t>(fabsf(d0)), m1 = static_cast<uint32_t>(fabsf(d1));
+        const uint32_t m2 = static_cast<uint32_t>(fabsf(d2)), m3 = static_cast<uint32_t>(fabsf(d3));
+        const uint32_t q  = it * 16 + (lane >> 1);
+        *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
+            make_uint2(__byte_perm(m0, m1, 0x5410) | (d0 < 0.0f ? 0x8000u : 0u), __byte_perm(m2, m3, 0x5410));
+        if (signw) {
+            // 4 sign bits per lane -> one u32 per 8 lanes (32 consecutive elements)
+            const uint32_t sgn = (d0 < 0.0f ? 1u : 0u) | (d1 < 0.0f ? 2u : 0u) | (d2 < 0.0f ? 4u : 0u) |
+                                 (d3 < 0.0f ? 8u : 0u);
+            uint32_t sv = sgn << ((lane & 7u) * 4);
+            sv |= __shfl_xor_sync(kFull, sv, 1);
+            sv |= __shfl_xor_sync(kFull, sv, 2);
+            sv |= __shfl_xor_sync(kFull, sv, 4);
+            if ((lane & 7u) == 0) signw[(base >> 5) + it * 4 + (lane >> 3)] = sv;
+        }
+        v = vn;
+        e0 += 128;
+    }
+    ovf |= (!(amax0 < 32768.0f) || !(amax1 < 65536.0f)) ? 1u : 0u;
+}
+
 // Plane/row/column of element e0 + 128 given that of e0 (x a multiple of 4).
 __device__ __forceinline__ void advance128_3d(const Geo& g, uint32_t e0, uint32_t& zz, uint32_t& yy,
                                               uint32_t& xx)
@@ -509,7 +554,9 @@ __device__ __forceinline__ void compute_block(const CompressArgs& a, const Geo& 
     const uint32_t base = t * kBlockCodes;
     if (t < a.nb) {
         // ---- phase A: codes of the block into shared memory (swizzled) ----
-        if (ND == 2 && g.al_x && base + kBlockCodes <= g.nl) {
+        if (ND == 1 && base + kBlockCodes <= g.nl) {
+            block1d(a.in, base, r, lane, sm, signw, ovf);
+        } else if (ND == 2 && g.al_x && base + kBlockCodes <= g.nl) {
             block2d(a.in, g, base, r, lane, sm, ovf);
         } else if (ND == 3 && g.al_x && base + kBlockCodes <= g.nl) {
             block3d(a.in, g, base, r, lane, sm, ovf);
