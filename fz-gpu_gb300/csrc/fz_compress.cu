@@ -244,6 +244,69 @@ __device__ __forceinline__ void block1d(const float* __restrict__ in, uint32_t b
     ovf |= (!(amax0 < 32768.0f) || !(amax1 < 65536.0f)) ? 1u : 0u;
 }
 
+// The 4 elements e0..e0+3 of a lane when rows are not a multiple of 4 elements long
+// (x >= 4: a group wraps a row at most once).  Position of each, from the first's.
+struct Pos4 {
+    uint32_t row[4], col[4];
+};
+__device__ __forceinline__ Pos4 pos4(const Geo& g, uint32_t row0, uint32_t col0)
+{
+    Pos4 P;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t c = col0 + j;
+        const bool     w = c >= g.x;
+        P.col[j]         = w ? c - g.x : c;
+        P.row[j]         = w ? row0 + 1 : row0;
+    }
+    return P;
+}
+
+// A whole 2D shuffle block inside x*y whose rows are not a multiple of 4 elements long
+// (x >= 4).  Same float expressions as the per-group path; the north row comes in four
+// coalesced scalar loads per group, the west neighbour of lane 0 is carried from lane 31
+// of the previous group row, and positions advance incrementally.
+__device__ __forceinline__ void block2d_u(const float* __restrict__ in, const Geo& g, uint32_t base, float r,
+                                          uint32_t lane, uint32_t* sm, uint32_t& ovf)
+{
+    uint32_t e0   = base + lane * 4;
+    uint32_t row0 = fdiv(e0, g.dx), col0 = e0 - row0 * g.x;
+    float    carry = 0.0f;  // t = c - n of element e0-1 (lane 0: the previous group row's last)
+    if (lane == 0 && (col0 & 15u))
+        carry = __fsub_rn(pq(__ldg(in + e0 - 1), r), (row0 & 15u) ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f);
+    float4 v    = ldg4(in + e0);
+    float  amax = 0.0f;
+#pragma unroll 2
+    for (uint32_t it = 0; it < 16; ++it) {
+        const float4 vn = it < 15 ? ldg4(in + e0 + 128) : v;
+        const Pos4   P  = pos4(g, row0, col0);
+        const float  c[4] = {v.x, v.y, v.z, v.w};
+        float        t[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float nq = (P.row[j] & 15u) ? pq(__ldg(in + (e0 + j - g.x)), r) : 0.0f;
+            t[j]           = __fsub_rn(pq(c[j], r), nq);
+        }
+        const float up = __shfl_up_sync(kFull, t[3], 1);
+        const float tw = lane ? up : carry;
+        carry          = __shfl_sync(kFull, t[3], 31);
+        float d[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float w = (P.col[j] & 15u) ? (j ? t[j - 1] : tw) : 0.0f;
+            d[j]          = __fsub_rn(t[j], w);
+            amax          = fmax_nan(amax, fabsf(d[j]));
+        }
+        const uint32_t q = it * 16 + (lane >> 1);
+        *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
+            make_uint2(pack_signed_pair(d[0], d[1]), pack_signed_pair(d[2], d[3]));
+        advance128(g, e0, row0, col0);
+        v = vn;
+        e0 += 128;
+    }
+    ovf |= !(amax < 32768.0f) ? 1u : 0u;
+}
+
 // Plane/row/column of element e0 + 128 given that of e0 (x a multiple of 4).
 __device__ __forceinline__ void advance128_3d(const Geo& g, uint32_t e0, uint32_t& zz, uint32_t& yy,
                                               uint32_t& xx)
@@ -260,6 +323,83 @@ __device__ __forceinline__ void advance128_3d(const Geo& g, uint32_t e0, uint32_
         const uint32_t rem = e - zz * g.xy;
         yy               = fdiv(rem, g.dx), xx = rem - yy * g.x;
     }
+}
+
+// A whole 3D shuffle block inside x*y*z whose rows are not a multiple of 4 elements long
+// (x >= 4: a lane's group wraps a row at most once).  Same float expressions as the
+// per-group path: halo values are zero where the element's tile has no such neighbour,
+// and the west terms of an element are its left neighbour's (same row whenever they are
+// used) -- for lane 0's first element carried from lane 31 of the previous group row.
+__device__ __forceinline__ void block3d_u(const float* __restrict__ in, const Geo& g, uint32_t base, float r,
+                                          uint32_t lane, uint32_t* sm, uint32_t& ovf)
+{
+    uint32_t e0 = base + lane * 4;
+    uint32_t zz = fdiv(e0, g.dxy);
+    uint32_t yy = fdiv(e0 - zz * g.xy, g.dx), xx = e0 - zz * g.xy - yy * g.x;
+    // prequantised c, n, b, bn of element e0-1 (lane 0's west neighbour, same row)
+    float cw = 0.0f, nw = 0.0f, bw = 0.0f, bnw = 0.0f;
+    if (lane == 0 && (xx & 7u)) {
+        const bool zi = (zz & 7u) != 0, yi = (yy & 7u) != 0;
+        cw  = pq(__ldg(in + e0 - 1), r);
+        nw  = yi ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f;
+        bw  = zi ? pq(__ldg(in + e0 - 1 - g.xy), r) : 0.0f;
+        bnw = (zi && yi) ? pq(__ldg(in + e0 - 1 - g.xy - g.x), r) : 0.0f;
+    }
+    float4 v    = ldg4(in + e0);
+    float  amax = 0.0f;
+#pragma unroll 1
+    for (uint32_t it = 0; it < 16; ++it) {
+        const float4 vn   = it < 15 ? ldg4(in + e0 + 128) : v;
+        const float  c[4] = {v.x, v.y, v.z, v.w};
+        float        p[4], nq[4], bq[4], bn[4];
+        bool         xi[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            uint32_t xj = xx + j, yj = yy, zj = zz;
+            if (xj >= g.x) {
+                xj -= g.x;
+                if (++yj == g.y) yj = 0, ++zj;
+            }
+            const bool     zi = (zj & 7u) != 0, yi = (yj & 7u) != 0;
+            const uint32_t e  = e0 + j;
+            xi[j]             = (xj & 7u) != 0;
+            p[j]              = pq(c[j], r);
+            nq[j]             = yi ? pq(__ldg(in + (e - g.x)), r) : 0.0f;
+            bq[j]             = zi ? pq(__ldg(in + (e - g.xy)), r) : 0.0f;
+            bn[j]             = (zi && yi) ? pq(__ldg(in + (e - g.xy - g.x)), r) : 0.0f;
+        }
+        float wp = __shfl_up_sync(kFull, p[3], 1), wn = __shfl_up_sync(kFull, nq[3], 1);
+        float wb = __shfl_up_sync(kFull, bq[3], 1), wbn = __shfl_up_sync(kFull, bn[3], 1);
+        if (lane == 0) wp = cw, wn = nw, wb = bw, wbn = bnw;
+        cw  = __shfl_sync(kFull, p[3], 31);
+        nw  = __shfl_sync(kFull, nq[3], 31);
+        bw  = __shfl_sync(kFull, bq[3], 31);
+        bnw = __shfl_sync(kFull, bn[3], 31);
+        float d[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            // c - (A - B - C - D + E + F + G), lorenzo_var.cuh:277-283; absent terms are 0
+            const float A = xi[j] ? (j ? bn[j - 1] : wbn) : 0.0f;
+            const float B = xi[j] ? (j ? nq[j - 1] : wn) : 0.0f;
+            const float C = xi[j] ? (j ? bq[j - 1] : wb) : 0.0f;
+            const float E = xi[j] ? (j ? p[j - 1] : wp) : 0.0f;
+            float       s = __fsub_rn(A, B);
+            s             = __fsub_rn(s, C);
+            s             = __fsub_rn(s, bn[j]);
+            s             = __fadd_rn(s, E);
+            s             = __fadd_rn(s, nq[j]);
+            s             = __fadd_rn(s, bq[j]);
+            d[j]          = __fsub_rn(p[j], s);
+            amax          = fmax_nan(amax, fabsf(d[j]));
+        }
+        const uint32_t q = it * 16 + (lane >> 1);
+        *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
+            make_uint2(pack_signed_pair(d[0], d[1]), pack_signed_pair(d[2], d[3]));
+        advance128_3d(g, e0, zz, yy, xx);
+        v = vn;
+        e0 += 128;
+    }
+    ovf |= !(amax < 32768.0f) ? 1u : 0u;
 }
 
 // A whole 3D shuffle block [base, base+2048) inside x*y*z with rows a multiple of 4
@@ -558,8 +698,12 @@ __device__ __forceinline__ void compute_block(const CompressArgs& a, const Geo& 
             block1d(a.in, base, r, lane, sm, signw, ovf);
         } else if (ND == 2 && g.al_x && base + kBlockCodes <= g.nl) {
             block2d(a.in, g, base, r, lane, sm, ovf);
+        } else if (ND == 2 && g.x >= 4 && base + kBlockCodes <= g.nl) {
+            block2d_u(a.in, g, base, r, lane, sm, ovf);
         } else if (ND == 3 && g.al_x && base + kBlockCodes <= g.nl) {
             block3d(a.in, g, base, r, lane, sm, ovf);
+        } else if (ND == 3 && g.x >= 4 && base + kBlockCodes <= g.nl) {
+            block3d_u(a.in, g, base, r, lane, sm, ovf);
         } else {
 #pragma unroll 4
             for (uint32_t it = 0; it < 16u; ++it) {
