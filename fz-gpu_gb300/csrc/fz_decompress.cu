@@ -174,6 +174,17 @@ __device__ __forceinline__ uint32_t sm_decode(uint32_t c)
     return (c & 0x8000u) ? 0u - mag : mag;
 }
 
+// Both sign-magnitude codes of a word w = c0 | c1 << 16 as two's-complement deltas.  An
+// arithmetic shift turns bit 15 (31) into an all-ones mask m, and (mag ^ m) - m is -mag
+// exactly when the sign is set -- sm_decode for both halves.
+__device__ __forceinline__ void sm_decode2(uint32_t w, uint32_t& d0, uint32_t& d1)
+{
+    const uint32_t m0 = static_cast<uint32_t>(static_cast<int32_t>(w << 16) >> 31);
+    const uint32_t m1 = static_cast<uint32_t>(static_cast<int32_t>(w) >> 31);
+    d0                = ((w & 0x7FFFu) ^ m0) - m0;
+    d1                = (((w >> 16) & 0x7FFFu) ^ m1) - m1;
+}
+
 // Decodes the 64 codes of group g (codes g*64 .. g*64+63) into 32 words w[j] =
 // code[2j] | code[2j+1] << 16.  Group gg of block b is word r4 = gg % 4 of the 32
 // chunks (p, k = gg / 4): its rank among the flagged chunks follows from the block's
@@ -248,8 +259,8 @@ __device__ __forceinline__ void rb_read4(const uint32_t* rb, uint32_t i, uint32_
 {
     if ((i & 3u) == 0) {
         const uint2 v = *reinterpret_cast<const uint2*>(rb + rb_chunk(i >> 6, (i >> 3) & 7u) + ((i >> 2) & 1u) * 2);
-        d[0] = sm_decode(v.x & 0xFFFFu), d[1] = sm_decode(v.x >> 16);
-        d[2] = sm_decode(v.y & 0xFFFFu), d[3] = sm_decode(v.y >> 16);
+        sm_decode2(v.x, d[0], d[1]);
+        sm_decode2(v.y, d[2], d[3]);
     } else {
 #pragma unroll
         for (uint32_t k = 0; k < 4; ++k) {
@@ -556,8 +567,8 @@ __global__ void __launch_bounds__(128) k_recon2d(const ReconArgs a, uint32_t nwi
         uint32_t     d[4] = {0, 0, 0, 0};
         if (vec) {
             const uint2 v = __ldg(reinterpret_cast<const uint2*>(a.codes + base));
-            d[0] = sm_decode(v.x & 0xFFFFu), d[1] = sm_decode(v.x >> 16);
-            d[2] = sm_decode(v.y & 0xFFFFu), d[3] = sm_decode(v.y >> 16);
+            sm_decode2(v.x, d[0], d[1]);
+            sm_decode2(v.y, d[2], d[3]);
         } else {
 #pragma unroll
             for (int j = 0; j < 4; ++j)
@@ -611,8 +622,8 @@ __global__ void __launch_bounds__(128) k_recon3d(const ReconArgs a, uint32_t nwi
             if (live) {
                 if (vec) {
                     const uint2 v = __ldg(reinterpret_cast<const uint2*>(a.codes + base));
-                    d[0] = sm_decode(v.x & 0xFFFFu), d[1] = sm_decode(v.x >> 16);
-                    d[2] = sm_decode(v.y & 0xFFFFu), d[3] = sm_decode(v.y >> 16);
+                    sm_decode2(v.x, d[0], d[1]);
+                    sm_decode2(v.y, d[2], d[3]);
                 } else {
 #pragma unroll
                     for (int j = 0; j < 4; ++j)
