@@ -74,6 +74,22 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(x, dist, device=None):
+    """Max of a float over all ranks of the process group (the value itself without one):
+    the timing rule of the multi-GPU run, so the slowest rank sets the step time."""
+    if not dist:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def rank_seed0(rank, fields):
+    """First field seed of a rank: every rank compresses its own fields (weak scaling)."""
+    return 1 + rank * fields
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -226,7 +242,7 @@ def run_fz(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     L = fz.lib()
-    fields = make_fields(args.fields, 1 + rank * args.fields)
+    fields = make_fields(args.fields, rank_seed0(rank, args.fields))
     n = fields[0].size
     cap = fz.max_compressed_bytes(n, DIMS, fz.MODE_SIDECAR)
     X = [torch.from_numpy(f).to(dev) for f in fields]
@@ -289,11 +305,7 @@ def run_fz(args, rank, world, local_rank):
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = t.item()
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, dev)
     gc.close(), gd.close()
     err = (Y[-1] - X[-1]).abs().max().item()
     assert err <= headers[-1].eb_abs * (1 + 2 ** -10) + 1e-6 * X[-1].abs().max().item(), err
@@ -439,10 +451,7 @@ def e2e(fz, L, fields, n, cap, sizes, args, dev, world, dist):
     for w in workers:
         if w["err"] is not None:
             raise w["err"]
-    if dist:
-        t = torch.tensor([el], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        el = t.item()
+    el = max_over_ranks(el, dist, dev)
     for w in workers:
         last = fields[w["last"]]
         err = float(np.max(np.abs(w["hout"].numpy().astype(np.float64) - last)))
