@@ -926,7 +926,7 @@ constexpr uint32_t kCompactBlocks = 32;   // shuffle blocks per k_compact CTA
 constexpr uint32_t kSuperBlocks   = 512;  // shuffle blocks per super-tile sum
 
 template <int ND>
-__global__ void __launch_bounds__(kCompressWarps * 32, 4) k_encode(const CompressArgs a, uint4* slots,
+__global__ void __launch_bounds__(kCompressWarps * 32, ND == 3 ? 4 : 5) k_encode(const CompressArgs a, uint4* slots,
                                                                     uint32_t* counts, uint32_t* supers,
                                                                     uint32_t* ovfw)
 {

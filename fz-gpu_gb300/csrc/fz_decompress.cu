@@ -295,7 +295,7 @@ __device__ __forceinline__ void store4(float* out, uint32_t lin, uint32_t live, 
 // shares with the next window) and the output once.
 constexpr uint32_t kW2 = 960;
 
-__global__ void __launch_bounds__(256) k_decompress2d(const DecodeArgs a, uint32_t nwin)
+__global__ void __launch_bounds__(256, 5) k_decompress2d(const DecodeArgs a, uint32_t nwin)
 {
     __shared__ __align__(16) uint32_t rows[16][512];  // 16 rows x 1024 codes
     const uint32_t tid = threadIdx.x;
