@@ -213,7 +213,7 @@ fz_status fz_workspace_bytes(uint64_t max_n, uint64_t* bytes)
     b += pad16(8 * tiles);          // state
     b += 64;                        // tickets, status, total
     b += 16;                        // range accumulators
-    b += pad16(2 * max_n + 16);     // decode scratch
+    b += pad16(2 * max_n + 16);     // per-block slots (k_encode)
     b += pad16(4 * tiles + 4);      // block offsets
     b += pad16(4 * (tiles / 512 + 2));  // chunk counts per 512 blocks
     *bytes = b;
@@ -390,7 +390,7 @@ fz_status fz::compress_impl(fz_workspace* ws, const float* d_in, uint64_t n, fz_
         a.ebh.range = a.ebh.vmin = a.ebh.vmax = 0.0f;
     }
     if (e == cudaSuccess) {
-        // two launches: per-block slots in the decode scratch (2 bytes per element, one 4 KiB
+        // two launches: per-block slots in the workspace scratch (2 bytes per element, one 4 KiB
         // slot per shuffle block) and per-block counts in the block-offset array
         KernelTimer t(ws, s, 1);
         e = launch_encode(a, reinterpret_cast<uint4*>(ws->codes), ws->boff, ws->supers, ws->ovfw, s);
@@ -436,7 +436,6 @@ fz_status fz_decompress(fz_workspace* ws, const void* d_stream, uint64_t stream_
 
     DecodeArgs d{};
     d.st    = static_cast<const uint8_t*>(d_stream);
-    d.codes = ws->codes;
     d.boff  = ws->boff;
     d.out   = d_out;
     d.n = L.n, d.nl = L.nl, d.x = L.x, d.y = L.y, d.z = L.z;
@@ -458,27 +457,7 @@ fz_status fz_decompress(fz_workspace* ws, const void* d_stream, uint64_t stream_
         KernelTimer t(ws, s, 3);
         e = launch_decompress_fused(d, s);
     }
-    if (e == cudaErrorNotSupported) {
-        // two-pass shapes (3D, rows not a multiple of 4): codes to scratch, then x_lorenzo
-        (void)cudaGetLastError();
-        {
-            KernelTimer t(ws, s, 3);
-            e = launch_decode(d, s);
-        }
-        if (e != cudaSuccess) return map_err(e);
-        ReconArgs r{};
-        r.codes    = ws->codes;
-        r.signbits = (L.ndim == 1 && L.mode == FZ_MODE_SIDECAR)
-                         ? reinterpret_cast<const uint32_t*>(d.st + L.off_sign) : nullptr;
-        r.signum = nullptr;
-        r.out    = d_out;
-        r.n = L.n, r.nl = L.nl, r.x = L.x, r.y = L.y, r.z = L.z;
-        r.ebx2 = h.ebx2;
-        KernelTimer t(ws, s, 4);
-        e = launch_reconstruct(r, s);
-    } else if (e == cudaSuccess && L.n > L.nl) {
-        e = launch_zero_tail(d_out, L.nl, L.n, s);
-    }
+    if (e == cudaSuccess && L.n > L.nl) e = launch_zero_tail(d_out, L.nl, L.n, s);
     return map_err(e);
 }
 

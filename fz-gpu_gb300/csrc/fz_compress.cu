@@ -1,18 +1,23 @@
 // fz_compress.cu -- compression kernels.
 //
 //   k_range       max - min of the field and the error-bound constants (fz.cu:137,
-//                 lorenzo_var.cuh:562-563), one pass, last-CTA finish.
-//   k_compress    the whole forward path in one pass: Lorenzo dual-quantisation
-//                 (lorenzo_var.cuh:47-295), bitshuffle + chunk flags + bitmap
-//                 (fz.cu:61-111), single-pass decoupled-lookback scan (replacing
-//                 cub::DeviceScan, fz.cu:187-201) and compaction (encodeDebug,
-//                 fz.cu:49-59).  Reads the field once, writes the stream once.
+//                 lorenzo_var.cuh:562-563), one pass.
+//   k_encode      Lorenzo dual-quantisation (lorenzo_var.cuh:47-295), bitshuffle +
+//                 chunk flags + bitmap (fz.cu:61-111) and each block's non-zero chunks
+//                 compacted into its own slot (encodeDebug, fz.cu:49-59); independent
+//                 CTAs, one 2048-code shuffle block per warp.
+//   k_compact     the prefix sum over the blocks' chunk counts (replacing
+//                 cub::DeviceScan, fz.cu:187-201) from per-512-block sums, the move of
+//                 the chunks to their final offsets, the offset table and the header.
+//   k_compress    the same forward path in a single launch with a decoupled look-back
+//                 over scan tiles (persistent, software pipelined); used where no
+//                 scratch for the slots exists (fz_compress_noalloc).
 //
 // Work decomposition: one warp owns one 2048-code shuffle block.  The warp computes its
 // codes from the floats (halo rows come from L2), stages them in 4 KiB of shared memory,
 // transposes 32x32 bit tiles in registers, derives the chunk flags with 8 ballots (which
-// are exactly the 8 bitmap words of the block), finds its output offset by look-back
-// over the preceding blocks and writes its non-zero chunks with 128-bit stores.
+// are exactly the 8 bitmap words of the block) and writes its non-zero chunks with
+// 128-bit stores.
 #include <algorithm>
 
 #include "fz_internal.h"

@@ -1,12 +1,15 @@
 // fz_decompress.cu -- decompression kernels (the inverse of fz_compress.cu).
 //
-//   k_decode   one warp per 2048-code shuffle block: popcounts of its 8 bitmap words,
-//              decoupled look-back for its first chunk, gather of the flagged 16-byte
-//              chunks (unflagged ones are zero), inverse 32x32 bit transposes, and a
-//              coalesced write of the 2048 codes.  The tail block copies the sidecar.
-//   k_recon    inverse Lorenzo on the codes: per-tile inclusive prefix sums in 32-bit
-//              integers (1D 256, 2D 16x16, 3D 8x8x8 -- the tiling of x_lorenzo_{1d,2d,
-//              3d}, lorenzo_var.cuh:297-518), then (float)p * ebx2.
+//   k_decompress1d/2d/3d  fused decode + inverse bitshuffle + inverse Lorenzo, from the
+//              stream straight into the field: each CTA decodes the 64-code groups its
+//              rows (or 256-element blocks) need -- rank of every flagged chunk from the
+//              bitmap and the block offset table, inverse 32x32 bit transposes -- then
+//              runs the per-tile inclusive prefix sums in 32-bit integers (1D 256, 2D
+//              16x16, 3D 8x8x8 -- the tiling of x_lorenzo_{1d,2d,3d},
+//              lorenzo_var.cuh:297-518) and writes (float)p * ebx2.
+//   k_offsets  block offset table from the bitmap (COMPAT streams, which carry none).
+//   k_recon{1,2,3}d  inverse Lorenzo of a code array (the stage-level API,
+//              fz_lorenzo_reconstruct).
 //
 // The reference has no working FZ decompressor (its x_lorenzo kernels read a separate
 // signum array that its compressor never writes), so this path is the exact inverse of
@@ -16,14 +19,6 @@
 #include "fz_internal.h"
 
 namespace fz {
-
-constexpr int kDecodeWarps = 8;
-
-__device__ __forceinline__ uint32_t swz_d(uint32_t q)
-{
-    const uint32_t g = q >> 3, t = q & 7u;
-    return ((g << 3) | (t ^ (g & 7u))) << 2;
-}
 
 // ------------------------------------------------------------- offsets --
 // boff[b] = chunks of blocks 0..b-1 (the exclusive scan fz.cu:187-192 restricted to
@@ -127,45 +122,6 @@ __device__ __forceinline__ void gather_block(const DecodeArgs& a, uint32_t t, ui
     }
     bad |= pre != end;  // bitmap and offset table disagree
     if (bad) atomicOr(a.status, kStatusCorrupt);
-}
-
-// Two-pass path (3D and unaligned 2D): codes of every shuffle block into a scratch array.
-__global__ void __launch_bounds__(kDecodeWarps * 32) k_decode(const DecodeArgs a)
-{
-    __shared__ __align__(16) uint32_t smem[kDecodeWarps][kBlockWords];
-    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-    const uint32_t t    = blockIdx.x * kDecodeWarps + wid;
-    uint32_t*      sm   = smem[wid];
-    if (t < a.nb) {
-        gather_block(a, t, lane, sm);
-        __syncwarp();
-        // un-shuffle: W[g*32 + j] bit p = S[p*32 + g] bit j (the transpose is an involution)
-        uint32_t w[32];
-#pragma unroll
-        for (uint32_t p = 0; p < 32; ++p) w[p] = sm[p * 32 + lane];
-        transpose32(w);
-        __syncwarp();
-#pragma unroll
-        for (uint32_t tt = 0; tt < 8; ++tt)
-            *reinterpret_cast<uint4*>(sm + swz_d(lane * 8 + tt)) =
-                make_uint4(w[4 * tt], w[4 * tt + 1], w[4 * tt + 2], w[4 * tt + 3]);
-        __syncwarp();
-        uint4* dst = reinterpret_cast<uint4*>(a.codes) + (size_t)t * 256;
-#pragma unroll
-        for (uint32_t i = 0; i < 8; ++i) dst[lane + 32 * i] = *reinterpret_cast<const uint4*>(sm + swz_d(lane + 32 * i));
-    } else if (t == a.nb && a.tail) {
-        // tail block: raw codes from the sidecar, or zeros without one
-        const uint16_t* src  = a.mode == 1 ? reinterpret_cast<const uint16_t*>(a.st + a.off_c) : nullptr;
-        uint16_t*       dstc = a.codes + (size_t)a.nb * kBlockCodes;
-        for (uint32_t i = lane; i < a.tail; i += 32) dstc[i] = src ? src[i] : (uint16_t)0;
-    }
-}
-
-cudaError_t launch_decode(const DecodeArgs& a, cudaStream_t s)
-{
-    const uint32_t ntiles = a.nb + (a.tail ? 1u : 0u);
-    k_decode<<<(uint32_t)cdiv(ntiles, kDecodeWarps), kDecodeWarps * 32, 0, s>>>(a);
-    return cudaGetLastError();
 }
 
 __device__ __forceinline__ uint32_t sm_decode(uint32_t c)

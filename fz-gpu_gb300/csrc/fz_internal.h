@@ -45,7 +45,6 @@ struct CompressArgs {
 
 struct DecodeArgs {
     const uint8_t*  st;
-    uint16_t*       codes;    // scratch u16[n] (two-pass path)
     const uint32_t* boff;     // chunk offset of each shuffle block (k_offsets)
     float*          out;      // fused paths
     uint32_t        n, nl, x, y, z, nb, tail, mode, nwords;
@@ -75,8 +74,7 @@ cudaError_t launch_compact(const CompressArgs& a, const uint4* slots, const uint
 cudaError_t launch_offsets(const uint8_t* st, uint64_t off_a, uint32_t nb, uint32_t nwords, uint64_t nnz,
                            uint32_t* boff, uint64_t* state, uint32_t* ticket, uint32_t* status,
                            uint32_t* epoch, cudaStream_t s);
-cudaError_t launch_decode(const DecodeArgs& a, cudaStream_t s);
-// fused decode + inverse Lorenzo; returns cudaErrorNotSupported for shapes it does not cover
+// fused decode + inverse Lorenzo (every shape)
 cudaError_t launch_decompress_fused(const DecodeArgs& a, cudaStream_t s);
 cudaError_t launch_reconstruct(const ReconArgs& a, cudaStream_t s);
 cudaError_t launch_zero_tail(float* out, uint32_t from, uint32_t n, cudaStream_t s);

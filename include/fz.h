@@ -132,8 +132,9 @@ fz_status fz_reference_sizes(uint64_t file_bytes, uint64_t nnz, uint64_t* origin
                              uint64_t* compressed, double* ratio);
 
 /* ------------------------------------------------------------ workspace -- */
-/* Device scratch for fields of up to max_n elements (scan state, range reduction,
-   decode scratch) plus a pinned host word for optional readbacks. */
+/* Device scratch for fields of up to max_n elements (scan state, range reduction, one
+   4 KiB slot per 2048-code block for compression, block counts and offsets; about 2.5
+   bytes per element) plus a pinned host word for optional readbacks. */
 fz_status fz_workspace_create(uint64_t max_n, fz_workspace** ws);
 fz_status fz_workspace_destroy(fz_workspace* ws);
 /* Device bytes a workspace for max_n elements allocates. */
