@@ -31,7 +31,7 @@ def _worker(rank, world, port, out):
 
 def test_max_over_ranks_and_disjoint_fields_gloo():
     world = 2
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of this (threaded) process
         out = m.dict()
         mp.spawn(_worker, args=(world, _free_port(), out), nprocs=world, join=True)
         got = dict(out)
