@@ -114,6 +114,7 @@ SIGNATURES = {
     "fz_batch_launch": (_I, [_P, _P]),
     "fz_batch_destroy": (_I, [_P]),
     "fz_batch_create_ex": (_I, [_P, _P, _U32, _I, _I, _I, _U32, C.POINTER(_P)]),
+    "fz_batch_create_pair": (_I, [_P, _P, _P, _U32, _I, _I, _U32, C.POINTER(_P)]),
     "fz_batch_autotune": (_I, [_P, _P, _U32, _I, _I, _I, _U32, _P, C.POINTER(_U32), C.POINTER(C.c_double)]),
     "fz_server_create": (_I, [_U64, _U32, _U64, C.POINTER(_P)]),
     "fz_server_submit": (_I, [_P, C.POINTER(Request)]),
@@ -424,6 +425,19 @@ class Batch:
                                                               EB_REL if rel else EB_ABS, mode, int(branches),
                                                               C.byref(h)))
         self.handle = h
+
+    @classmethod
+    def pair(cls, ws, comp, dec, rel=True, mode=MODE_SIDECAR, branches=0):
+        """Round-trip batch (fz_batch_create_pair): comp[i] compressed, then dec[i]
+        decompressed, per field on one branch."""
+        self = cls.__new__(cls)
+        self.ws, self.fields = ws, (comp, dec)
+        h = C.c_void_p()
+        _check("fz_batch_create_pair", lib().fz_batch_create_pair(ws.handle, comp, dec, len(comp),
+                                                                  EB_REL if rel else EB_ABS, mode, int(branches),
+                                                                  C.byref(h)))
+        self.handle = h
+        return self
 
     def launch(self, stream=None):
         _check("fz_batch_launch", lib().fz_batch_launch(self.handle, _stream_handle(stream)))

@@ -650,17 +650,18 @@ fz_status fz_batch_create(fz_workspace* ws, const fz_field* fields, uint32_t cou
     return fz_batch_create_ex(ws, fields, count, dir, eb_mode, mode, 0, out);
 }
 
-fz_status fz_batch_create_ex(fz_workspace* ws, const fz_field* fields, uint32_t count, fz_direction dir,
-                             fz_eb_mode eb_mode, fz_mode mode, uint32_t nbranch, fz_batch** out)
+// Captures count fields into one graph: comp[i] (compression, if comp) followed by
+// dec[i] (decompression, if dec) on branch i % branches, each branch with its own
+// workspace; the fork and the join make the graph one unit on the launching stream.
+static fz_status capture_batch(fz_workspace* ws, const fz_field* comp, const fz_field* dec, uint32_t count,
+                               fz_eb_mode eb_mode, fz_mode mode, uint32_t nbranch, fz_batch* b)
 {
-    if (!ws || !out || (!fields && count) || (dir != FZ_COMPRESS && dir != FZ_DECOMPRESS)) return FZ_INVALID_ARG;
-    if (nbranch > FZ_BATCH_MAX_BRANCHES) return FZ_INVALID_ARG;
-    *out = nullptr;
-    fz_batch* b = new (std::nothrow) fz_batch();
-    if (!b) return FZ_FAIL_GPU_MALLOC;
     const uint32_t branches = std::max(1u, std::min(nbranch ? nbranch : kBatchBranches, count));
     uint64_t       max_n    = 1;
-    for (uint32_t i = 0; i < count; ++i) max_n = std::max<uint64_t>(max_n, dir == FZ_COMPRESS ? fields[i].n : fields[i].header.n);
+    for (uint32_t i = 0; i < count; ++i) {
+        if (comp) max_n = std::max<uint64_t>(max_n, comp[i].n);
+        if (dec) max_n = std::max<uint64_t>(max_n, dec[i].header.n);
+    }
     std::vector<fz_workspace*> wss{ws};
     fz_status                  st = FZ_SUCCESS;
     for (uint32_t i = 1; i < branches && st == FZ_SUCCESS; ++i) {
@@ -688,8 +689,8 @@ fz_status fz_batch_create_ex(fz_workspace* ws, const fz_field* fields, uint32_t 
             for (uint32_t i = 0; i < count && st == FZ_SUCCESS; ++i) {
                 const uint32_t k = i % branches;
                 fz_stream_t    h = reinterpret_cast<fz_stream_t>(cs[k]);
-                st = dir == FZ_COMPRESS ? fz_compress_batch(wss[k], fields + i, 1, eb_mode, mode, h)
-                                        : fz_decompress_batch(wss[k], fields + i, 1, h);
+                if (comp) st = fz_compress_batch(wss[k], comp + i, 1, eb_mode, mode, h);
+                if (dec && st == FZ_SUCCESS) st = fz_decompress_batch(wss[k], dec + i, 1, h);
             }
             // join
             for (uint32_t i = 1; i < branches; ++i) {
@@ -711,6 +712,36 @@ fz_status fz_batch_create_ex(fz_workspace* ws, const fz_field* fields, uint32_t 
         if (cs[i]) cudaStreamDestroy(cs[i]);
         if (ev[i]) cudaEventDestroy(ev[i]);
     }
+    return st;
+}
+
+fz_status fz_batch_create_ex(fz_workspace* ws, const fz_field* fields, uint32_t count, fz_direction dir,
+                             fz_eb_mode eb_mode, fz_mode mode, uint32_t nbranch, fz_batch** out)
+{
+    if (!ws || !out || (!fields && count) || (dir != FZ_COMPRESS && dir != FZ_DECOMPRESS)) return FZ_INVALID_ARG;
+    if (nbranch > FZ_BATCH_MAX_BRANCHES) return FZ_INVALID_ARG;
+    *out = nullptr;
+    fz_batch* b = new (std::nothrow) fz_batch();
+    if (!b) return FZ_FAIL_GPU_MALLOC;
+    const fz_status st = capture_batch(ws, dir == FZ_COMPRESS ? fields : nullptr, dir == FZ_DECOMPRESS ? fields : nullptr,
+                                       count, eb_mode, mode, nbranch, b);
+    if (st != FZ_SUCCESS) {
+        fz_batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_batch_create_pair(fz_workspace* ws, const fz_field* comp, const fz_field* dec, uint32_t count,
+                               fz_eb_mode eb_mode, fz_mode mode, uint32_t nbranch, fz_batch** out)
+{
+    if (!ws || !out || ((!comp || !dec) && count)) return FZ_INVALID_ARG;
+    if (nbranch > FZ_BATCH_MAX_BRANCHES) return FZ_INVALID_ARG;
+    *out = nullptr;
+    fz_batch* b = new (std::nothrow) fz_batch();
+    if (!b) return FZ_FAIL_GPU_MALLOC;
+    const fz_status st = capture_batch(ws, comp, dec, count, eb_mode, mode, nbranch, b);
     if (st != FZ_SUCCESS) {
         fz_batch_destroy(b);
         return st;

@@ -284,6 +284,15 @@ fz_status fz_batch_create_ex(fz_workspace* ws, const fz_field* fields, uint32_t 
                              fz_direction dir, fz_eb_mode eb_mode, fz_mode mode, uint32_t branches,
                              fz_batch** out);
 
+/* A round-trip batch (no counterpart in the reference): field i is compressed from
+   comp[i] and then decompressed from dec[i] (dec[i].src is normally comp[i].dst, with
+   dec[i].header taken from a compression of the same data), the pairs on up to
+   `branches` parallel branches (0 = 8) of one graph, so one field's decompression
+   overlaps other fields' compression.  Replays with the same inputs reproduce the same
+   streams, so the captured headers stay valid. */
+fz_status fz_batch_create_pair(fz_workspace* ws, const fz_field* comp, const fz_field* dec, uint32_t count,
+                               fz_eb_mode eb_mode, fz_mode mode, uint32_t branches, fz_batch** out);
+
 /* Autotuner for batch scheduling (no counterpart in the reference).  The stream format
    fixes the shuffle block and the Lorenzo tiles, so what is tuned is how many fields run
    side by side: captures the batch with 1, 2, 4, 8 and 16 branches (capped at `count`),

@@ -360,3 +360,28 @@ def test_compaction_group_boundaries(fz, oracle, ws, nblocks, extra):
         assert_same_stream(got, want)
         rec = fz.decompress(st, ws=ws).cpu().numpy()
         assert np.array_equal(rec.view(np.uint32), oracle.decompress(want).view(np.uint32))
+
+
+def test_round_trip_pair_batch(fz, oracle, synth):
+    """fz_batch_create_pair: each field compressed then decompressed on one branch of one
+    graph; every replay reproduces the oracle's streams and reconstructions."""
+    items = _mixed_fields(synth)
+    ws = fz.Workspace(max(d.size for d, _, _ in items))
+    xs, ss, ys, comp = _batch_buffers(fz, items)
+    wants = [oracle.compress(d, dims, eb) for d, dims, eb in items]
+    dec = fz.fields_array([{"src": s.data_ptr(), "dst": y.data_ptr(), "src_bytes": w.size, "dst_capacity": y.numel(),
+                            "header": fz.parse_header(w)} for s, y, w in zip(ss, ys, wants)])
+    for branches in (1, 2, 16):
+        g = fz.Batch.pair(ws, comp, dec, branches=branches)
+        for _ in range(2):
+            for s in ss:
+                s.fill_(0x5A)
+            for y in ys:
+                y.fill_(3.0)
+            g.launch()
+            torch.cuda.synchronize()
+            for s, y, w in zip(ss, ys, wants):
+                assert_same_stream(s[: w.size].cpu().numpy(), w)
+                assert np.array_equal(y.cpu().numpy().view(np.uint32), oracle.decompress(w).view(np.uint32))
+        g.close()
+    assert ws.status() == fz.SUCCESS
