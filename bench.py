@@ -397,9 +397,15 @@ def run_fz(args, rank, world, local_rank):
     if rank == 0 and world == 1:
         import oracle
         oracle.build()
+        cores = oracle.threads()
         gbs, reps, el = cpu_round_trips(fields[0], args.cpu_seconds)
-        line["cpu_baseline"] = {"value": round(gbs, 3), "unit": "GB/s", "cores": oracle.threads(),
-                                "kind": "port", "sample": f"{reps} round trips of one {'x'.join(map(str, DIMS))} field ({el:.1f} s)"}
+        # the same round trips on one thread (a short sample)
+        oracle.set_threads(1)
+        gbs1, reps1, el1 = cpu_round_trips(fields[0], max(0.2, args.cpu_seconds / 4), min_reps=1)
+        oracle.set_threads(cores)
+        line["cpu_baseline"] = {"value": round(gbs, 3), "unit": "GB/s", "cores": cores,
+                                "kind": "port", "sample": f"{reps} round trips of one {'x'.join(map(str, DIMS))} field ({el:.1f} s)",
+                                "one_thread": {"value": round(gbs1, 3), "sample": f"{reps1} round trips ({el1:.1f} s)"}}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

@@ -603,7 +603,8 @@ constexpr int kRangeUnroll = 8;
 // to "empty" for the next call.  Each thread issues kRangeUnroll 16-byte loads at once
 // (coalesced across the CTA); the grid covers the field in one batch per thread, so the
 // block scheduler keeps every SM streaming until the last CTAs.  NaN/Inf raise
-// kStatusNonfinite.
+// kStatusNonfinite: the running min and max propagate NaN (min.NaN / max.NaN), so one
+// test of each thread's final pair finds any NaN, -Inf or +Inf it has seen.
 __global__ void __launch_bounds__(256) k_range(const float* __restrict__ in, uint32_t n, uint32_t* mm,
                                                uint32_t* status)
 {
@@ -620,11 +621,13 @@ __global__ void __launch_bounds__(256) k_range(const float* __restrict__ in, uin
 #pragma unroll
         for (int k = 0; k < kRangeUnroll; ++k) {
             if (b + k * blockDim.x >= n4) continue;
-            mn = fminf(fminf(mn, v[k].x), fminf(v[k].y, fminf(v[k].z, v[k].w)));
-            mx = fmaxf(fmaxf(mx, v[k].x), fmaxf(v[k].y, fmaxf(v[k].z, v[k].w)));
-            nonfinite |= !isfinite(v[k].x) | !isfinite(v[k].y) | !isfinite(v[k].z) | !isfinite(v[k].w);
+            mn = fmin_nan(fmin_nan(mn, v[k].x), fmin_nan(v[k].y, fmin_nan(v[k].z, v[k].w)));
+            mx = fmax_nan(fmax_nan(mx, v[k].x), fmax_nan(v[k].y, fmax_nan(v[k].z, v[k].w)));
         }
     }
+    // NaN leaves both NaN; -Inf shows in the min, +Inf in the max (the start values
+    // +Inf / -Inf of a thread without elements stay on the other side)
+    nonfinite = (mn != mn) | (mn == -INFINITY) | (mx == INFINITY);
     if (blockIdx.x == 0 && threadIdx.x < n - 4 * n4) {
         const float v = in[4 * n4 + threadIdx.x];
         mn = fminf(mn, v), mx = fmaxf(mx, v);

@@ -275,6 +275,7 @@ __global__ void __launch_bounds__(256, 5) k_decompress2d(const DecodeArgs a, uin
     const bool     live = col < c1;
     const uint32_t q    = tid & 3u;
     uint32_t       acc[4] = {0, 0, 0, 0};
+#pragma unroll 4
     for (uint32_t rr = 0; rr < 16; ++rr) {
         const uint32_t row = r0 + rr;
         if (row >= a.y) break;  // uniform across the CTA

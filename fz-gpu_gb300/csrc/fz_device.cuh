@@ -98,6 +98,12 @@ __device__ __forceinline__ float fmax_nan(float a, float b)
     asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
     return r;
 }
+__device__ __forceinline__ float fmin_nan(float a, float b)
+{
+    float r;
+    asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
 // 1D positions i%4 != 0 store the magnitude only (lorenzo_var.cuh:62).
 __device__ __forceinline__ uint32_t pack_unsigned(float d)
 {

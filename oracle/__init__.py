@@ -64,6 +64,8 @@ def lib():
             L.fzo_decompress.argtypes = [p, u64, p, u64]
             L.fzo_metrics.argtypes = [p, p, u64, p, p, p, p]
             L.fzo_threads.restype = C.c_int
+            L.fzo_set_threads.restype = None
+            L.fzo_set_threads.argtypes = [C.c_int]
             _lib = L
     return _lib
 
@@ -82,6 +84,11 @@ def ndim(x, y, z):
 
 def threads():
     return lib().fzo_threads()
+
+
+def set_threads(n: int):
+    """Threads of the oracle's parallel loops from now on (calling thread)."""
+    lib().fzo_set_threads(int(n))
 
 
 def value_range(data):

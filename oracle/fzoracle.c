@@ -35,6 +35,15 @@ int fzo_threads(void)
 #endif
 }
 
+void fzo_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
 /* lorenzo_var.cuh:537-544: 1D iff z==1 and y==1, 2D iff z==1, else 3D. */
 int fzo_ndim(uint32_t x, uint32_t y, uint32_t z)
 {

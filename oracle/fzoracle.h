@@ -73,6 +73,8 @@ void fzo_metrics(const float* orig, const float* recon, uint64_t n, double* max_
 
 /* OpenMP thread count used (1 when built without OpenMP). */
 int fzo_threads(void);
+/* Threads of the following parallel regions of the calling thread (OpenMP). */
+void fzo_set_threads(int n);
 
 #ifdef __cplusplus
 }

@@ -206,6 +206,23 @@ def test_workspace_reuse_across_calls(fz, oracle, synth, ws):
             assert_same_stream(got, want)
 
 
+@pytest.mark.parametrize("n", [5001, (1 << 22) + 3])
+def test_nonfinite_input_relative_bound(fz, oracle, synth, ws, n):
+    """NaN, +Inf or -Inf anywhere in a field (first element, middle, the last elements past
+    the 16-byte loads) makes a relative-bound compression return FZ_NONFINITE_INPUT; the
+    workspace then compresses a finite field exactly as the oracle does."""
+    base = synth.smooth1d(n, seed=5)
+    for bad in (np.nan, np.inf, -np.inf):
+        for pos in (0, n // 2 + 1, n - 1, n - 4):
+            x = base.copy()
+            x[pos] = bad
+            with pytest.raises(fz.FzError) as e:
+                fz.compress(torch.from_numpy(x).cuda(), (n, 1, 1), 1e-3, rel=True, ws=ws)
+            assert e.value.status == fz.NONFINITE_INPUT, (bad, pos)
+        st, got, want = run_both(fz, oracle, ws, base, (n, 1, 1), 1e-3)
+        assert_same_stream(got, want)
+
+
 def test_errors_are_statuses(fz, ws):
     x = torch.zeros(4096 + 4, device="cuda")
     out = torch.empty(1 << 16, dtype=torch.uint8, device="cuda")
