@@ -13,9 +13,9 @@ is visited once per step, so each step reads its inputs from HBM.
   value      uncompressed GB/s through the codec, both directions:
              steps * fields * 2 * 4n bytes / device time (CUDA events), summed over ranks
   e2e        the same metric through the host-buffer C-ABI calls fz_compress_host /
-             fz_decompress_host (pinned host memory, H2D and D2H copies inside the region),
-             issued from eight host threads with a workspace each so that one field's
-             input copy overlaps another's output copy on the host link
+             fz_decompress_host (pinned host memory, H2D and D2H copies inside the region):
+             eight compressing host threads hand their streams to eight decompressing
+             ones, so input copies and output copies share the host link at all times
   roofline   the dominant kernel's algorithmic bytes per launch / its mean event-timed
              launch duration, against the measured HBM copy bandwidth
   cpu_baseline  the oracle (C, OpenMP) on this host's cores, round trips of one field
@@ -412,78 +412,116 @@ def run_fz(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
-# host threads issuing e2e round trips (one per field of a step): with several in flight
-# the host link carries H2D and D2H at once (measured 210 + 193 GB/s one-way, 339 both)
+# host threads on each side of the e2e pipeline: compressing threads hand their streams
+# to decompressing threads, so input copies (H2D) and output copies (D2H) run at once on
+# the host link (measured 210 + 193 GB/s one-way, 339 both)
 E2E_THREADS = int(os.environ.get("FZ_E2E_THREADS", "8"))
 
 
 def e2e(fz, L, fields, n, cap, sizes, args, dev, world, dist):
-    """Host-buffer round trips through fz_compress_host / fz_decompress_host, issued
-    from E2E_THREADS host threads, each with its own workspace, stream and pinned
-    staging buffers (the calls release the GIL), so one field's input copy (H2D) runs
-    beside another's output copy (D2H)."""
-    import threading
+    """Host-buffer round trips through fz_compress_host / fz_decompress_host.
+
+    E2E_THREADS compressing threads (a workspace and stream each) take the step's fields
+    in turn from pinned host memory and compress each into a pinned stream buffer of a
+    shared pool; E2E_THREADS decompressing threads take the finished streams in order
+    and decompress each back into pinned host memory.  The calls release the GIL.  Every
+    field is compressed and decompressed once per step; the region ends when the last
+    decompression has returned."""
+    import queue
     import numpy as np
     import torch
     steps = min(args.steps, 30)
+    nf = len(fields)
+    items = steps * nf
+    T = E2E_THREADS
     hin = [torch.from_numpy(f).pin_memory() for f in fields]
     dims = fz._dims(DIMS)
-    workers = []
-    for _ in range(E2E_THREADS):
-        workers.append({"ws": fz.Workspace(n), "st": torch.cuda.Stream(dev),
-                        "hst": torch.empty(cap, dtype=torch.uint8).pin_memory(),
-                        "hout": torch.empty(n, dtype=torch.float32).pin_memory(), "bytes": 0, "err": None})
+    free, ready = queue.Queue(), queue.Queue()
+    for _ in range(2 * T):
+        free.put(torch.empty(cap, dtype=torch.uint8).pin_memory())
+    cw = [{"ws": fz.Workspace(n), "st": torch.cuda.Stream(dev), "bytes": 0, "err": None} for _ in range(T)]
+    dw = [{"ws": fz.Workspace(n), "st": torch.cuda.Stream(dev), "last": None, "err": None,
+           "hout": torch.empty(n, dtype=torch.float32).pin_memory()} for _ in range(T)]
 
-    def one(w, i):
+    def compress(w, i, buf):
         nb = C.c_uint64()
-        sh = C.c_void_p(w["st"].cuda_stream)
         st = L.fz_compress_host(w["ws"].handle, C.c_void_p(hin[i].data_ptr()), n, dims, EB, fz.EB_REL,
-                                fz.MODE_SIDECAR, C.c_void_p(w["hst"].data_ptr()), cap, C.byref(nb), sh)
-        st |= L.fz_decompress_host(w["ws"].handle, C.c_void_p(w["hst"].data_ptr()), nb.value,
-                                   C.c_void_p(w["hout"].data_ptr()), n, sh)
+                                fz.MODE_SIDECAR, C.c_void_p(buf.data_ptr()), cap, C.byref(nb),
+                                C.c_void_p(w["st"].cuda_stream))
         if st:
-            raise fz.FzError("e2e", st)
+            raise fz.FzError("e2e compress", st)
         return nb.value
 
-    items = steps * len(fields)
+    def decompress(w, buf, nbytes):
+        st = L.fz_decompress_host(w["ws"].handle, C.c_void_p(buf.data_ptr()), nbytes,
+                                  C.c_void_p(w["hout"].data_ptr()), n, C.c_void_p(w["st"].cuda_stream))
+        if st:
+            raise fz.FzError("e2e decompress", st)
 
-    def run(k):
-        w = workers[k]
+    def run_compress(k):
+        w = cw[k]
         torch.cuda.set_device(dev)
         try:
-            for j in range(k, items, E2E_THREADS):
-                w["bytes"] += one(w, j % len(fields))
-                w["last"] = j % len(fields)
+            for j in range(k, items, T):
+                buf = free.get(timeout=120)  # raises if the decompressing side has stopped
+                nb = compress(w, j % nf, buf)
+                w["bytes"] += nb
+                ready.put((buf, nb, j % nf))
         except Exception as ex:  # surfaced after join
             w["err"] = ex
+            ready.put(None)
 
-    for k, w in enumerate(workers):
-        one(w, k % len(fields))
+    def run_decompress(k):
+        w = dw[k]
+        torch.cuda.set_device(dev)
+        try:
+            while True:
+                it = ready.get(timeout=120)
+                if it is None:
+                    return
+                buf, nb, i = it
+                decompress(w, buf, nb)
+                w["last"] = i
+                free.put(buf)
+        except Exception as ex:
+            w["err"] = ex
+
+    # warm-up: every workspace allocates its staging buffers
+    buf = free.get()
+    for w in cw:
+        nb = compress(w, 0, buf)
+    for w in dw:
+        decompress(w, buf, nb)
+    free.put(buf)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    th = [threading.Thread(target=run, args=(k,)) for k in range(E2E_THREADS)]
-    for t in th:
+    tc = [threading.Thread(target=run_compress, args=(k,)) for k in range(T)]
+    td = [threading.Thread(target=run_decompress, args=(k,)) for k in range(T)]
+    for t in tc + td:
         t.start()
-    for t in th:
+    for t in tc:
+        t.join()
+    for _ in td:
+        ready.put(None)
+    for t in td:
         t.join()
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
-    for w in workers:
+    for w in cw + dw:
         if w["err"] is not None:
             raise w["err"]
     el = max_over_ranks(el, dist, dev)
-    for w in workers:
+    for w in dw:
         last = fields[w["last"]]
         err = float(np.max(np.abs(w["hout"].numpy().astype(np.float64) - last)))
         assert err <= 1e-3 * float(np.float32(last.max() - last.min())) * 1.001, err
-    total_stream = sum(w["bytes"] for w in workers)
-    per_step_stream = total_stream / steps
-    return {"value": round(len(fields) * 2 * 4 * n * steps * world / el / 1e9, 2), "unit": "GB/s",
-            "steps": steps, "host_threads": E2E_THREADS,
-            "h2d_bytes_per_step": int(len(fields) * 4 * n + per_step_stream),
-            "d2h_bytes_per_step": int(per_step_stream + len(fields) * 4 * n)}
+    per_step_stream = sum(w["bytes"] for w in cw) / steps
+    return {"value": round(nf * 2 * 4 * n * steps * world / el / 1e9, 2), "unit": "GB/s",
+            "steps": steps, "host_threads": {"compress": T, "decompress": T},
+            "h2d_bytes_per_step": int(nf * 4 * n + per_step_stream),
+            "d2h_bytes_per_step": int(per_step_stream + nf * 4 * n)}
 
 
 def _torch_fields(specs, dev):
