@@ -137,6 +137,26 @@ __device__ __forceinline__ uint32_t swz(uint32_t q)
     return ((g << 3) | (t ^ (g & 7u))) << 2;
 }
 
+// Store offsets of the whole-block paths.  Group row it of a lane writes its 4 codes (one
+// half of chunk q = 16 it + lane/2) at word swz(q) + 2 (lane & 1) = 64 it + x(it % 4), with
+// x(k) = 32 h + 2 (lane & 1) + 4 (tq ^ (2k + h)), h = lane / 16, tq = (lane / 2) % 8.  The
+// four values rotate by one per group row: a loop unrolled by 4 keeps them in registers
+// and adds 64 it as an immediate offset.
+struct SwzRot {
+    uint32_t x0, x1, x2, x3;
+    __device__ __forceinline__ explicit SwzRot(uint32_t lane)
+    {
+        const uint32_t h = lane >> 4, tq = (lane >> 1) & 7u, lo = (h << 5) + (lane & 1u) * 2;
+        x0 = lo + ((tq ^ h) << 2), x1 = lo + ((tq ^ (2u + h)) << 2);
+        x2 = lo + ((tq ^ (4u + h)) << 2), x3 = lo + ((tq ^ (6u + h)) << 2);
+    }
+    __device__ __forceinline__ void next()
+    {
+        const uint32_t t = x0;
+        x0 = x1, x1 = x2, x2 = x3, x3 = t;
+    }
+};
+
 // Position (row, col) of element e0 + 128 given that of e0 (x a multiple of 4).
 __device__ __forceinline__ void advance128(const Geo& g, uint32_t e0, uint32_t& row, uint32_t& col)
 {
@@ -152,32 +172,32 @@ __device__ __forceinline__ void advance128(const Geo& g, uint32_t e0, uint32_t& 
 // are a multiple of 4 elements long (so a group of 4 never straddles a row and halo rows
 // are 16-byte aligned).  Same float expressions as fast2d; the west neighbour's t of lane
 // 0 is carried from lane 31 of the previous group row, row/column advance incrementally,
-// and the loads run two group rows ahead of the arithmetic.  The north row is zero
-// outside the tile, so its prequantised values need no select.
+// and the next group row's loads are issued before the current one is processed (a
+// two-stage rotation, so unrolling by 4 leaves no register moves and folds the swizzled
+// store offsets).  The north row is zero outside the tile, so its prequantised values
+// need no select.
 __device__ __forceinline__ void block2d(const float* __restrict__ in, const Geo& g, uint32_t base, float r,
                                         uint32_t lane, uint32_t* sm, uint32_t& ovf)
 {
     const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     uint32_t     e0 = base + lane * 4;
     uint32_t     row0 = fdiv(e0, g.dx), col0 = e0 - row0 * g.x;
-    uint32_t     row1 = row0, col1 = col0;
-    advance128(g, e0, row1, col1);
-    float4 v0 = ldg4(in + e0), u0 = (row0 & 15u) ? ldg4(in + (e0 - g.x)) : z4;
-    float4 v1 = ldg4(in + e0 + 128), u1 = (row1 & 15u) ? ldg4(in + (e0 + 128 - g.x)) : z4;
+    float4       v0 = ldg4(in + e0), u0 = (row0 & 15u) ? ldg4(in + (e0 - g.x)) : z4;
     // t = c - n of element base-1, the west neighbour of lane 0's first group
     float carry = 0.0f;
     if (lane == 0 && (col0 & 15u))
         carry = __fsub_rn(pq(__ldg(in + e0 - 1), r), (row0 & 15u) ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f);
-    float amax = 0.0f;  // max |d| (NaN if any d is NaN)
-#pragma unroll 2
+    SwzRot       so(lane);
+    float        amax = 0.0f;  // max |d| (NaN if any d is NaN)
+#pragma unroll 4
     for (uint32_t it = 0; it < 16; ++it) {
-        // group row it+2 of this lane: 256 elements on
-        uint32_t row2 = row1, col2 = col1;
-        float4   v2 = z4, u2 = z4;
-        if (it < 14) {
-            advance128(g, e0 + 128, row2, col2);
-            v2 = ldg4(in + e0 + 256);
-            if (row2 & 15u) u2 = ldg4(in + (e0 + 256 - g.x));
+        // group row it+1 of this lane: 128 elements on
+        uint32_t row1 = row0, col1 = col0;
+        float4   v1 = z4, u1 = z4;
+        if (it < 15) {
+            advance128(g, e0, row1, col1);
+            v1 = ldg4(in + e0 + 128);
+            if (row1 & 15u) u1 = ldg4(in + (e0 + 128 - g.x));
         }
         const bool cin = (col0 & 15u) != 0;
         float      t[4];
@@ -194,11 +214,10 @@ __device__ __forceinline__ void block2d(const float* __restrict__ in, const Geo&
             d[j] = __fsub_rn(t[j], j ? t[j - 1] : tw);
             amax = fmax_nan(amax, fabsf(d[j]));
         }
-        const uint32_t q = it * 16 + (lane >> 1);
-        *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
+        *reinterpret_cast<uint2*>(sm + it * 64 + so.x0) =
             make_uint2(pack_signed_pair(d[0], d[1]), pack_signed_pair(d[2], d[3]));
+        so.next();
         v0 = v1, u0 = u1, row0 = row1, col0 = col1;
-        v1 = v2, u1 = u2, row1 = row2, col1 = col2;
         e0 += 128;
     }
     ovf |= !(amax < 32768.0f) ? 1u : 0u;
@@ -218,7 +237,8 @@ __device__ __forceinline__ void block1d(const float* __restrict__ in, uint32_t b
     float4   v     = ldg4(in + e0);
     float    carry = 0.0f;
     float    amax0 = 0.0f, amax1 = 0.0f;  // max |d| of the signed / magnitude-only positions
-#pragma unroll 2
+    SwzRot   so(lane);
+#pragma unroll 4
     for (uint32_t it = 0; it < 16; ++it) {
         const float4 vn = it < 15 ? ldg4(in + e0 + 128) : v;
         const float  p0 = pq(v.x, r), p1 = pq(v.y, r), p2 = pq(v.z, r), p3 = pq(v.w, r);
@@ -230,9 +250,9 @@ __device__ __forceinline__ void block1d(const float* __restrict__ in, uint32_t b
         amax1          = fmax_nan(amax1, fmax_nan(fabsf(d1), fmax_nan(fabsf(d2), fabsf(d3))));
         const uint32_t m0 = static_cast<uint32_t>(fabsf(d0)), m1 = static_cast<uint32_t>(fabsf(d1));
         const uint32_t m2 = static_cast<uint32_t>(fabsf(d2)), m3 = static_cast<uint32_t>(fabsf(d3));
-        const uint32_t q  = it * 16 + (lane >> 1);
-        *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
+        *reinterpret_cast<uint2*>(sm + it * 64 + so.x0) =
             make_uint2(__byte_perm(m0, m1, 0x5410) | (d0 < 0.0f ? 0x8000u : 0u), __byte_perm(m2, m3, 0x5410));
+        so.next();
         if (signw) {
             // 4 sign bits per lane -> one u32 per 8 lanes (32 consecutive elements)
             const uint32_t sgn = (d0 < 0.0f ? 1u : 0u) | (d1 < 0.0f ? 2u : 0u) | (d2 < 0.0f ? 4u : 0u) |
@@ -281,7 +301,8 @@ __device__ __forceinline__ void block2d_u(const float* __restrict__ in, const Ge
         carry = __fsub_rn(pq(__ldg(in + e0 - 1), r), (row0 & 15u) ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f);
     float4 v    = ldg4(in + e0);
     float  amax = 0.0f;
-#pragma unroll 2
+    SwzRot so(lane);
+#pragma unroll 4
     for (uint32_t it = 0; it < 16; ++it) {
         const float4 vn = it < 15 ? ldg4(in + e0 + 128) : v;
         const Pos4   P  = pos4(g, row0, col0);
@@ -302,9 +323,9 @@ __device__ __forceinline__ void block2d_u(const float* __restrict__ in, const Ge
             d[j]          = __fsub_rn(t[j], w);
             amax          = fmax_nan(amax, fabsf(d[j]));
         }
-        const uint32_t q = it * 16 + (lane >> 1);
-        *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
+        *reinterpret_cast<uint2*>(sm + it * 64 + so.x0) =
             make_uint2(pack_signed_pair(d[0], d[1]), pack_signed_pair(d[2], d[3]));
+        so.next();
         advance128(g, e0, row0, col0);
         v = vn;
         e0 += 128;
