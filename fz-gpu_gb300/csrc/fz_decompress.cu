@@ -15,6 +15,7 @@
 // signum array that its compressor never writes), so this path is the exact inverse of
 // the compressed format rather than a restatement.
 #include <algorithm>
+#include <atomic>
 
 #include "fz_internal.h"
 
@@ -198,30 +199,56 @@ __device__ __forceinline__ void decode_group(const DecodeArgs& a, uint32_t g, ui
 }
 
 // Decoded row buffers (fused 2D/3D paths): a row of the field's window is held as 64-code
-// slots (one decode group each) of eight 16-byte chunks; chunk c of slot G sits at chunk
-// position c ^ (G & 7), so the 16-byte stores of neighbouring groups spread over the banks.
-__device__ __forceinline__ uint32_t rb_chunk(uint32_t G, uint32_t c) { return (G * 8 + (c ^ (G & 7u))) << 2; }
+// slots (one decode group each) of eight 16-byte chunks, in one of two layouts:
+//   padded (2D): code e at word (e / 64) * kSlotWords + (e % 64) / 2.  The 16-byte pad
+//     per slot puts neighbouring slots 4 banks apart, so the 16-byte stores of 8 threads
+//     writing chunk tt of consecutive groups hit distinct banks, and a read address is a
+//     shift, a mask and a multiply-add.
+//   swizzled (3D, whose kernel runs at its register limit): 32 words per slot, chunk c of
+//     slot G at chunk position c ^ (G & 7).
+constexpr uint32_t kSlotWords = 36;
 
+template <bool kPad>
+__device__ __forceinline__ uint32_t rb_slot_words()
+{
+    return kPad ? kSlotWords : 32u;
+}
+// word of chunk c of slot G
+template <bool kPad>
+__device__ __forceinline__ uint32_t rb_chunk(uint32_t G, uint32_t c)
+{
+    return kPad ? G * kSlotWords + 4 * c : (G * 8 + (c ^ (G & 7u))) << 2;
+}
+// word holding code e
+template <bool kPad>
+__device__ __forceinline__ uint32_t rb_word(uint32_t e)
+{
+    return kPad ? (e >> 6) * kSlotWords + ((e & 63u) >> 1) : rb_chunk<false>(e >> 6, (e >> 3) & 7u) + ((e >> 1) & 3u);
+}
+
+template <bool kPad>
 __device__ __forceinline__ void rb_put_group(uint32_t* rb, uint32_t j, const uint32_t (&w)[32])
 {
 #pragma unroll
     for (uint32_t tt = 0; tt < 8; ++tt)
-        *reinterpret_cast<uint4*>(rb + rb_chunk(j, tt)) = make_uint4(w[4 * tt], w[4 * tt + 1], w[4 * tt + 2], w[4 * tt + 3]);
+        *reinterpret_cast<uint4*>(rb + rb_chunk<kPad>(j, tt)) =
+            make_uint4(w[4 * tt], w[4 * tt + 1], w[4 * tt + 2], w[4 * tt + 3]);
 }
 
 // Integer deltas of codes i..i+3 of a row buffer.  i % 4 is the same for every thread of
 // a row, so the branch is uniform.
+template <bool kPad>
 __device__ __forceinline__ void rb_read4(const uint32_t* rb, uint32_t i, uint32_t (&d)[4])
 {
     if ((i & 3u) == 0) {
-        const uint2 v = *reinterpret_cast<const uint2*>(rb + rb_chunk(i >> 6, (i >> 3) & 7u) + ((i >> 2) & 1u) * 2);
+        const uint2 v = *reinterpret_cast<const uint2*>(rb + rb_word<kPad>(i));
         sm_decode2(v.x, d[0], d[1]);
         sm_decode2(v.y, d[2], d[3]);
     } else {
 #pragma unroll
         for (uint32_t k = 0; k < 4; ++k) {
             const uint32_t e  = i + k;
-            const uint32_t wv = rb[rb_chunk(e >> 6, (e >> 3) & 7u) + ((e >> 1) & 3u)];
+            const uint32_t wv = rb[rb_word<kPad>(e)];
             d[k]              = sm_decode((e & 1u) ? wv >> 16 : wv & 0xFFFFu);
         }
     }
@@ -253,7 +280,7 @@ constexpr uint32_t kW2 = 960;
 
 __global__ void __launch_bounds__(256, 5) k_decompress2d(const DecodeArgs a, uint32_t nwin)
 {
-    __shared__ __align__(16) uint32_t rows[16][512];  // 16 rows x 1024 codes
+    __shared__ __align__(16) uint32_t rows[16][16 * kSlotWords];  // 16 rows x 16 slots of 64 codes
     const uint32_t tid = threadIdx.x;
     const uint32_t bx = blockIdx.x % nwin, by = blockIdx.x / nwin;
     const uint32_t c0 = bx * kW2, c1 = min(c0 + kW2, a.x);
@@ -266,7 +293,7 @@ __global__ void __launch_bounds__(256, 5) k_decompress2d(const DecodeArgs a, uin
             if (g <= ((lin1 - 1) >> 6)) {
                 uint32_t w[32];
                 decode_group(a, g, w);
-                rb_put_group(rows[rr], j, w);
+                rb_put_group<true>(rows[rr], j, w);
             }
         }
     }
@@ -281,7 +308,7 @@ __global__ void __launch_bounds__(256, 5) k_decompress2d(const DecodeArgs a, uin
         if (row >= a.y) break;  // uniform across the CTA
         const uint32_t lin0 = row * a.x + c0;
         uint32_t       d[4] = {0, 0, 0, 0};
-        if (live) rb_read4(rows[rr], (lin0 & 63u) + 4 * tid, d);
+        if (live) rb_read4<true>(rows[rr], (lin0 & 63u) + 4 * tid, d);
         d[1] += d[0], d[2] += d[1], d[3] += d[2];
         uint32_t v = d[3];
         uint32_t u = __shfl_up_sync(kFull, v, 1);
@@ -304,7 +331,8 @@ __global__ void __launch_bounds__(256, 5) k_decompress2d(const DecodeArgs a, uin
 // slots ("span" mode, no group decoded twice inside the CTA); otherwise each of the
 // bands x 8 rows of a plane gets its own buffer of g slots.  Phase 2: thread (band, cq)
 // owns columns 4cq..4cq+3 of its band; prefix along x within the 8-column tile row (pair
-// shuffle), running sum along y within the plane, running sum along z in zacc, then the
+// shuffle), running sum along y within the plane, running sum along z in shared memory
+// (one 16-byte slot per thread and row: in registers they would spill), then the
 // stores.
 struct Brick3 {
     uint32_t w, q2, bands, g;  // window columns, column quads, bands per CTA, slots per row
@@ -313,7 +341,7 @@ struct Brick3 {
 };
 constexpr uint32_t kW3 = 960;
 
-__global__ void __launch_bounds__(256, 3) k_decompress3d(const DecodeArgs a, const Brick3 k)
+__global__ void __launch_bounds__(256, 4) k_decompress3d(const DecodeArgs a, const Brick3 k)
 {
     extern __shared__ __align__(16) uint32_t rb3[];
     const uint32_t tid = threadIdx.x;
@@ -328,9 +356,10 @@ __global__ void __launch_bounds__(256, 3) k_decompress3d(const DecodeArgs a, con
     // buffer words per plane (span) or per row
     const uint32_t rowwords = (k.span ? k.pg : k.g) * 32;
     const uint32_t ntask    = k.span ? 2 * k.pg : k.bands * 16 * k.g;
-    uint32_t       zacc[8][4];
+    // running sums along z, one 16-byte slot per thread and row of its band (after the row buffers)
+    uint4* zs = reinterpret_cast<uint4*>(rb3 + (k.span ? 2 * k.pg : k.bands * 16 * k.g) * 32) + tid;
 #pragma unroll
-    for (int yy = 0; yy < 8; ++yy) zacc[yy][0] = zacc[yy][1] = zacc[yy][2] = zacc[yy][3] = 0;
+    for (int yy = 0; yy < 8; ++yy) zs[yy * 256] = make_uint4(0, 0, 0, 0);
     for (uint32_t pz = 0; pz < 8; pz += 2) {
         if (z0 + pz >= a.z) break;  // uniform across the CTA
         for (uint32_t task = tid; task < ntask; task += 256) {
@@ -350,7 +379,7 @@ __global__ void __launch_bounds__(256, 3) k_decompress3d(const DecodeArgs a, con
             if (g > ((lin1 - 1) >> 6)) continue;
             uint32_t w[32];
             decode_group(a, g, w);
-            rb_put_group(rb3 + r * rowwords, j, w);
+            rb_put_group<false>(rb3 + r * rowwords, j, w);
         }
         __syncthreads();
         for (uint32_t p = 0; p < 2; ++p) {
@@ -365,18 +394,21 @@ __global__ void __launch_bounds__(256, 3) k_decompress3d(const DecodeArgs a, con
                 const uint32_t lin0 = (zz * a.y + yv) * a.x + c0;
                 uint32_t       d[4] = {0, 0, 0, 0};
                 if (live) {
-                    if (k.span) rb_read4(rb3 + p * rowwords, lin0 + 4 * cq - pbase, d);
-                    else rb_read4(rb3 + (band * 16 + p * 8 + yy) * rowwords, (lin0 & 63u) + 4 * cq, d);
+                    if (k.span) rb_read4<false>(rb3 + p * rowwords, lin0 + 4 * cq - pbase, d);
+                    else rb_read4<false>(rb3 + (band * 16 + p * 8 + yy) * rowwords, (lin0 & 63u) + 4 * cq, d);
                 }
                 d[1] += d[0], d[2] += d[1], d[3] += d[2];
                 const uint32_t u  = __shfl_up_sync(kFull, d[3], 1);
                 const uint32_t ex = (cq & 1u) ? u : 0u;
+                const uint4    z4 = zs[yy * 256];
+                uint32_t       zv[4] = {z4.x, z4.y, z4.z, z4.w};
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     colacc[j] += d[j] + ex;
-                    zacc[yy][j] += colacc[j];
+                    zv[j] += colacc[j];
                 }
-                if (live) store4(a.out, lin0 + 4 * cq, c1 - col, zacc[yy], a.ebx2);
+                zs[yy * 256] = make_uint4(zv[0], zv[1], zv[2], zv[3]);
+                if (live) store4(a.out, lin0 + 4 * cq, c1 - col, zv, a.ebx2);
             }
         }
         __syncthreads();
@@ -412,7 +444,28 @@ static Brick3 brick3(uint32_t x, uint32_t y)
     return k;
 }
 
-static uint32_t brick3_smem(const Brick3& k) { return k.span ? 2 * k.pg * 128 : k.bands * 16 * k.g * 128; }
+// Dynamic shared memory of a k_decompress3d CTA: the row buffers (span mode at most 2 x 122
+// slots, otherwise at most 48 KB) and the z sums (8 rows x 256 threads x 16 bytes).
+constexpr uint32_t kDecompress3dSmemMax = 48 * 1024 + 8 * 256 * 16;
+
+static uint32_t brick3_smem(const Brick3& k)
+{
+    return (k.span ? 2 * k.pg * 128 : k.bands * 16 * k.g * 128) + 8 * 256 * 16;
+}
+
+// Above 48 KB a kernel's dynamic shared memory needs an opt-in, which is per device.
+static cudaError_t allow_decompress3d_smem()
+{
+    static std::atomic<uint64_t> done{0};  // bit d: opted in on device d
+    int         dev = 0;
+    cudaError_t e   = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev < 64 ? 1ull << dev : 0ull;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(k_decompress3d, cudaFuncAttributeMaxDynamicSharedMemorySize, kDecompress3dSmemMax);
+    if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
+    return e;
+}
 
 // ------------------------------------------------------ fused 1D decode --
 // One warp per shuffle block: lane g decodes its 64 codes (a quarter of one 256-element
@@ -495,7 +548,10 @@ cudaError_t launch_decompress_fused(const DecodeArgs& a, cudaStream_t s)
         return cudaGetLastError();
     }
     if (nd == 3) {
+        const cudaError_t e = allow_decompress3d_smem();
+        if (e != cudaSuccess) return e;
         const Brick3   k    = brick3(a.x, a.y);
+        if (brick3_smem(k) > kDecompress3dSmemMax) return cudaErrorInvalidConfiguration;
         const uint64_t ctas = (uint64_t)k.nwin * k.nbgrp * cdiv(a.z, 8);
         k_decompress3d<<<(uint32_t)ctas, 256, brick3_smem(k), s>>>(a, k);
         return cudaGetLastError();
