@@ -3,7 +3,7 @@
 
 A step is one pass of the path over one batch of synthetic input: `--fields` (8)
 independent exafel-like 39200x388 float32 fields (the single-field workload the metric
-is quoted on; configs[1], relative eb 1e-3), each compressed (range pass, encode,
+is quoted on, relative eb 1e-3), each compressed (range pass, encode,
 compaction) and then decompressed (fused decode + inverse Lorenzo) on the device,
 issued as one CUDA-graph replay (fz_batch_create_pair: each field's compression and
 then its decompression on one of several parallel branches).  The
@@ -61,8 +61,8 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--workload", choices=["exafel", "batch", "serving"], default="exafel",
-                   help="exafel: the headline line (single-field workload, see --field); batch: configs[3]; "
-                        "serving: configs[4]")
+                   help="exafel: the headline line (single-field workload, see --field); batch: 512 mixed "
+                        "1D/2D/3D fields batched vs per field; serving: a Poisson request trace")
     p.add_argument("--field", choices=sorted(FIELDS), default="exafel",
                    help="the single-field workload of the headline line (default exafel)")
     p.add_argument("--batch-fields", type=int, default=512)
@@ -533,7 +533,7 @@ def _torch_fields(specs, dev):
 
 
 def run_batch(args, local_rank):
-    """configs[3]: a mixed batch (log-uniform 64 KB-256 MB, 1D/2D/3D, eb from
+    """A mixed batch of 512 fields (log-uniform 64 KB-256 MB, 1D/2D/3D, eb from
     {1e-2,1e-3,1e-4}) compressed and decompressed from two CUDA-graph replays, against the
     plain per-field path (fz_compress with its size readback, then fz_decompress)."""
     import importlib
@@ -587,7 +587,7 @@ def run_batch(args, local_rank):
     # every stream of the replays equals the plain path's (which tests check bit for bit)
     assert all(fz.parse_header(s_[:64].cpu().numpy()).nnz == h.nnz for s_, h in zip(S[:8], heads[:8]))
     ratio = sum(4 * n for n in ns) / sum(sizes)
-    line = {"metric": "configs[3]: batched vs per-field aggregate GB/s (compress + decompress)",
+    line = {"metric": "512 mixed fields: batched vs per-field aggregate GB/s (compress + decompress)",
             "value": round(2 * total / t_batch / 1e9, 2), "unit": "GB/s",
             "per_field_plain": round(2 * total / t_plain / 1e9, 2),
             "speedup_vs_per_field": round(t_plain / t_batch, 2),
@@ -603,8 +603,8 @@ def run_batch(args, local_rank):
 
 
 def run_serving(args, local_rank):
-    """configs[4]: Poisson arrivals (mean --serve-rate req/s) of fields drawn as in
-    configs[3], 60/40 compress/decompress, served by the request loop (8 slots, HBM
+    """Poisson arrivals (mean --serve-rate req/s) of fields drawn as in the mixed batch,
+    60/40 compress/decompress, served by the request loop (8 slots, HBM
     budget) against the same trace served one request at a time (1 slot).  Two request
     kinds: device-resident fields (FZ_REQUEST_DEVICE, the fields and results live in HBM)
     and host buffers (pinned; H2D/D2H copies per request)."""
@@ -712,11 +712,11 @@ def run_serving(args, local_rank):
     plain_gbs = plain()
     dev_mode["saturated_gbs"]["plain_per_field"] = round(plain_gbs, 2)
     dev_mode["saturated_gbs"]["speedup_vs_plain"] = round(dev_mode["saturated_gbs"]["slots8"] / plain_gbs, 2)
-    line = {"metric": "configs[4]: served latency and aggregate GB/s (uncompressed bytes)",
+    line = {"metric": "Poisson request trace: served latency and aggregate GB/s (uncompressed bytes)",
             "requests": nreq, "rate_req_s": args.serve_rate, "hbm_budget_gb": round(budget / 2 ** 30, 1),
             **dev_mode, "host_buffers": mode(False),
             "data": "synthetic (seeded device-side generators, 48 distinct fields)",
-            "config": {"workload": "Poisson arrivals, 60/40 compress/decompress, fields as configs[3]",
+            "config": {"workload": "Poisson arrivals, 60/40 compress/decompress, fields as in the mixed batch",
                        "requests": "device-resident fields and results (FZ_REQUEST_DEVICE); "
                                    "host_buffers: the same trace with pinned host buffers"}}
     print(json.dumps(line), flush=True)

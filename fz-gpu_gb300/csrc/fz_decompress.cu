@@ -208,11 +208,6 @@ __device__ __forceinline__ void decode_group(const DecodeArgs& a, uint32_t g, ui
 //     slot G at chunk position c ^ (G & 7).
 constexpr uint32_t kSlotWords = 36;
 
-template <bool kPad>
-__device__ __forceinline__ uint32_t rb_slot_words()
-{
-    return kPad ? kSlotWords : 32u;
-}
 // word of chunk c of slot G
 template <bool kPad>
 __device__ __forceinline__ uint32_t rb_chunk(uint32_t G, uint32_t c)

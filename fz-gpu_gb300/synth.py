@@ -29,7 +29,7 @@ def _plane_waves_2d(x, y, rng, terms, lam_lo, lam_hi):
 
 
 def smooth2d(x, y, seed=0, zero_frac=0.30, noise=1e-4):
-    """configs[0]: 16 random 2D sinusoids (wavelength 50-1000 cells) normalised to
+    """cesm-like 3600x1800 field: 16 random 2D sinusoids (wavelength 50-1000 cells) normalised to
     [0,1], ~30% exact zeros in contiguous patches (thresholded low-frequency mask),
     N(0, 1e-4) noise, clipped at 0."""
     rng = np.random.default_rng(seed)
@@ -44,7 +44,7 @@ def smooth2d(x, y, seed=0, zero_frac=0.30, noise=1e-4):
 
 
 def peaks2d(x, y, seed=1, npeaks=None):
-    """configs[1]: Gaussian(0, 0.5) background plus ~2000 seeded 2D Gaussian peaks
+    """exafel-like 39200x388 field: Gaussian(0, 0.5) background plus ~2000 seeded 2D Gaussian peaks
     (sigma 1-3 px, amplitude log-uniform 10-1e4), a heavy-tailed value range."""
     rng = np.random.default_rng(seed)
     f = rng.normal(0.0, 0.5, size=(y, x)).astype(np.float32)
@@ -66,7 +66,7 @@ def peaks2d(x, y, seed=1, npeaks=None):
 
 
 def smooth3d(x, y, z, seed=2, zero_frac=0.40):
-    """configs[2]: 32 random 3D sinusoids plus a seeded vortex-like radial profile,
+    """hurricane-like 500x500x100 field: 32 random 3D sinusoids plus a seeded vortex-like radial profile,
     ~40% of voxels exactly 0 (values below the 40th percentile are cut to 0)."""
     rng = np.random.default_rng(seed)
     xs = np.arange(x, dtype=np.float32)
@@ -143,7 +143,7 @@ def _dims_for(n, nd, rng):
 
 
 def mixed_specs(count, seed=3, lo_bytes=64 << 10, hi_bytes=256 << 20, ebs=(1e-2, 1e-3, 1e-4)):
-    """configs[3]/[4]: `count` fields with sizes log-uniform between 64 KB and 256 MB,
+    """The mixed batch and the request trace: `count` fields with sizes log-uniform between 64 KB and 256 MB,
     mixed 1D/2D/3D, each with an eb drawn from {1e-2, 1e-3, 1e-4}.  Returns
     [(kind, dims, eb, seed)]."""
     rng = np.random.default_rng(seed)
