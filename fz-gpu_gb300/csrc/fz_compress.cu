@@ -187,8 +187,9 @@ __device__ __forceinline__ void block2d(const float* __restrict__ in, const Geo&
     float carry = 0.0f;
     if (lane == 0 && (col0 & 15u))
         carry = __fsub_rn(pq(__ldg(in + e0 - 1), r), (row0 & 15u) ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f);
-    SwzRot       so(lane);
-    float        amax = 0.0f;  // max |d| (NaN if any d is NaN)
+    SwzRot         so(lane);
+    const uint32_t prev = (lane + 31u) & 31u;
+    float          amax = 0.0f;  // max |d| (NaN if any d is NaN)
 #pragma unroll 4
     for (uint32_t it = 0; it < 16; ++it) {
         // group row it+1 of this lane: 128 elements on
@@ -205,15 +206,15 @@ __device__ __forceinline__ void block2d(const float* __restrict__ in, const Geo&
         t[1] = __fsub_rn(pq(v0.y, r), pq(u0.y, r));
         t[2] = __fsub_rn(pq(v0.z, r), pq(u0.z, r));
         t[3] = __fsub_rn(pq(v0.w, r), pq(u0.w, r));
-        const float up = __shfl_up_sync(kFull, t[3], 1);
-        const float tw = cin ? (lane ? up : carry) : 0.0f;
-        carry          = __shfl_sync(kFull, t[3], 31);
+        // lane l - 1's t[3]; lane 0 gets lane 31's, its west neighbour one group row on
+        const float rot = __shfl_sync(kFull, t[3], prev);
+        const float tw  = cin ? (lane ? rot : carry) : 0.0f;
+        carry           = rot;
         float d[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            d[j] = __fsub_rn(t[j], j ? t[j - 1] : tw);
-            amax = fmax_nan(amax, fabsf(d[j]));
-        }
+        for (int j = 0; j < 4; ++j) d[j] = __fsub_rn(t[j], j ? t[j - 1] : tw);
+        amax = fmax3_nan(amax, fabsf(d[0]), fabsf(d[1]));
+        amax = fmax3_nan(amax, fabsf(d[2]), fabsf(d[3]));
         *reinterpret_cast<uint2*>(sm + it * 64 + so.x0) =
             make_uint2(pack_signed_pair(d[0], d[1]), pack_signed_pair(d[2], d[3]));
         so.next();
@@ -237,17 +238,18 @@ __device__ __forceinline__ void block1d(const float* __restrict__ in, uint32_t b
     float4   v     = ldg4(in + e0);
     float    carry = 0.0f;
     float    amax0 = 0.0f, amax1 = 0.0f;  // max |d| of the signed / magnitude-only positions
-    SwzRot   so(lane);
+    SwzRot         so(lane);
+    const uint32_t prev = (lane + 31u) & 31u;
 #pragma unroll 4
     for (uint32_t it = 0; it < 16; ++it) {
         const float4 vn = it < 15 ? ldg4(in + e0 + 128) : v;
         const float  p0 = pq(v.x, r), p1 = pq(v.y, r), p2 = pq(v.z, r), p3 = pq(v.w, r);
-        const float  up = __shfl_up_sync(kFull, p3, 1);
-        const float  w  = (e0 & 255u) ? (lane ? up : carry) : 0.0f;
-        carry           = __shfl_sync(kFull, p3, 31);
+        const float  rot = __shfl_sync(kFull, p3, prev);  // lane 0: lane 31's, for the next group row
+        const float  w   = (e0 & 255u) ? (lane ? rot : carry) : 0.0f;
+        carry            = rot;
         const float d0 = __fsub_rn(p0, w), d1 = __fsub_rn(p1, p0), d2 = __fsub_rn(p2, p1), d3 = __fsub_rn(p3, p2);
         amax0          = fmax_nan(amax0, fabsf(d0));
-        amax1          = fmax_nan(amax1, fmax_nan(fabsf(d1), fmax_nan(fabsf(d2), fabsf(d3))));
+        amax1          = fmax_nan(amax1, fmax3_nan(fabsf(d1), fabsf(d2), fabsf(d3)));
         const uint32_t m0 = static_cast<uint32_t>(fabsf(d0)), m1 = static_cast<uint32_t>(fabsf(d1));
         const uint32_t m2 = static_cast<uint32_t>(fabsf(d2)), m3 = static_cast<uint32_t>(fabsf(d3));
         *reinterpret_cast<uint2*>(sm + it * 64 + so.x0) =
@@ -300,8 +302,9 @@ __device__ __forceinline__ void block2d_u(const float* __restrict__ in, const Ge
     if (lane == 0 && (col0 & 15u))
         carry = __fsub_rn(pq(__ldg(in + e0 - 1), r), (row0 & 15u) ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f);
     float4 v    = ldg4(in + e0);
-    float  amax = 0.0f;
-    SwzRot so(lane);
+    float          amax = 0.0f;
+    SwzRot         so(lane);
+    const uint32_t prev = (lane + 31u) & 31u;
 #pragma unroll 4
     for (uint32_t it = 0; it < 16; ++it) {
         const float4 vn = it < 15 ? ldg4(in + e0 + 128) : v;
@@ -313,9 +316,9 @@ __device__ __forceinline__ void block2d_u(const float* __restrict__ in, const Ge
             const float nq = (P.row[j] & 15u) ? pq(__ldg(in + (e0 + j - g.x)), r) : 0.0f;
             t[j]           = __fsub_rn(pq(c[j], r), nq);
         }
-        const float up = __shfl_up_sync(kFull, t[3], 1);
-        const float tw = lane ? up : carry;
-        carry          = __shfl_sync(kFull, t[3], 31);
+        const float rot = __shfl_sync(kFull, t[3], prev);  // lane 0: lane 31's, for the next group row
+        const float tw  = lane ? rot : carry;
+        carry           = rot;
         float d[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {

@@ -98,6 +98,13 @@ __device__ __forceinline__ float fmax_nan(float a, float b)
     asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
     return r;
 }
+// max(a, b, c) with NaN propagation (the three-input max.NaN.f32 of sm_100 and later).
+__device__ __forceinline__ float fmax3_nan(float a, float b, float c)
+{
+    float r;
+    asm("max.NaN.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
 __device__ __forceinline__ float fmin_nan(float a, float b)
 {
     float r;
