@@ -374,8 +374,9 @@ __device__ __forceinline__ void block3d_u(const float* __restrict__ in, const Ge
         bw  = zi ? pq(__ldg(in + e0 - 1 - g.xy), r) : 0.0f;
         bnw = (zi && yi) ? pq(__ldg(in + e0 - 1 - g.xy - g.x), r) : 0.0f;
     }
-    float4 v    = ldg4(in + e0);
-    float  amax = 0.0f;
+    float4         v    = ldg4(in + e0);
+    float          amax = 0.0f;
+    const uint32_t prev = (lane + 31u) & 31u;
 #pragma unroll 1
     for (uint32_t it = 0; it < 16; ++it) {
         const float4 vn   = it < 15 ? ldg4(in + e0 + 128) : v;
@@ -397,13 +398,11 @@ __device__ __forceinline__ void block3d_u(const float* __restrict__ in, const Ge
             bq[j]             = zi ? pq(__ldg(in + (e - g.xy)), r) : 0.0f;
             bn[j]             = (zi && yi) ? pq(__ldg(in + (e - g.xy - g.x)), r) : 0.0f;
         }
-        float wp = __shfl_up_sync(kFull, p[3], 1), wn = __shfl_up_sync(kFull, nq[3], 1);
-        float wb = __shfl_up_sync(kFull, bq[3], 1), wbn = __shfl_up_sync(kFull, bn[3], 1);
-        if (lane == 0) wp = cw, wn = nw, wb = bw, wbn = bnw;
-        cw  = __shfl_sync(kFull, p[3], 31);
-        nw  = __shfl_sync(kFull, nq[3], 31);
-        bw  = __shfl_sync(kFull, bq[3], 31);
-        bnw = __shfl_sync(kFull, bn[3], 31);
+        // lane l - 1's values; lane 0 gets lane 31's, its west neighbours one group row on
+        const float rp = __shfl_sync(kFull, p[3], prev), rn = __shfl_sync(kFull, nq[3], prev);
+        const float rb = __shfl_sync(kFull, bq[3], prev), rbn = __shfl_sync(kFull, bn[3], prev);
+        float       wp = lane ? rp : cw, wn = lane ? rn : nw, wb = lane ? rb : bw, wbn = lane ? rbn : bnw;
+        cw = rp, nw = rn, bw = rb, bnw = rbn;
         float d[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -419,8 +418,9 @@ __device__ __forceinline__ void block3d_u(const float* __restrict__ in, const Ge
             s             = __fadd_rn(s, nq[j]);
             s             = __fadd_rn(s, bq[j]);
             d[j]          = __fsub_rn(p[j], s);
-            amax          = fmax_nan(amax, fabsf(d[j]));
         }
+        amax = fmax3_nan(amax, fabsf(d[0]), fabsf(d[1]));
+        amax = fmax3_nan(amax, fabsf(d[2]), fabsf(d[3]));
         const uint32_t q = it * 16 + (lane >> 1);
         *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
             make_uint2(pack_signed_pair(d[0], d[1]), pack_signed_pair(d[2], d[3]));
@@ -457,7 +457,8 @@ __device__ __forceinline__ void block3d(const float* __restrict__ in, const Geo&
         bw  = zi ? pq(__ldg(in + e0 - 1 - g.xy), r) : 0.0f;
         bnw = (zi && yi) ? pq(__ldg(in + e0 - 1 - g.xy - g.x), r) : 0.0f;
     }
-    float amax = 0.0f;  // max |d| (NaN if any d is NaN)
+    float          amax = 0.0f;  // max |d| (NaN if any d is NaN)
+    const uint32_t prev = (lane + 31u) & 31u;
 #pragma unroll 1
     for (uint32_t it = 0; it < 16; ++it) {
         uint32_t zn = zz, yn = yy, xn = xx;
@@ -475,13 +476,11 @@ __device__ __forceinline__ void block3d(const float* __restrict__ in, const Geo&
         const float nq[4] = {pq(un.x, r), pq(un.y, r), pq(un.z, r), pq(un.w, r)};
         const float bq[4] = {pq(ub.x, r), pq(ub.y, r), pq(ub.z, r), pq(ub.w, r)};
         const float bn[4] = {pq(uc.x, r), pq(uc.y, r), pq(uc.z, r), pq(uc.w, r)};
-        float       wp = __shfl_up_sync(kFull, p[3], 1), wn = __shfl_up_sync(kFull, nq[3], 1);
-        float       wb = __shfl_up_sync(kFull, bq[3], 1), wbn = __shfl_up_sync(kFull, bn[3], 1);
-        if (lane == 0) wp = cw, wn = nw, wb = bw, wbn = bnw;
-        cw  = __shfl_sync(kFull, p[3], 31);
-        nw  = __shfl_sync(kFull, nq[3], 31);
-        bw  = __shfl_sync(kFull, bq[3], 31);
-        bnw = __shfl_sync(kFull, bn[3], 31);
+        // lane l - 1's values; lane 0 gets lane 31's, its west neighbours one group row on
+        const float rp = __shfl_sync(kFull, p[3], prev), rn = __shfl_sync(kFull, nq[3], prev);
+        const float rb = __shfl_sync(kFull, bq[3], prev), rbn = __shfl_sync(kFull, bn[3], prev);
+        float       wp = lane ? rp : cw, wn = lane ? rn : nw, wb = lane ? rb : bw, wbn = lane ? rbn : bnw;
+        cw = rp, nw = rn, bw = rb, bnw = rbn;
         if ((xx & 7u) == 0) wp = wn = wb = wbn = 0.0f;  // the group starts a tile row
         float d[4];
 #pragma unroll
@@ -494,8 +493,9 @@ __device__ __forceinline__ void block3d(const float* __restrict__ in, const Geo&
             s       = __fadd_rn(s, nq[j]);
             s       = __fadd_rn(s, bq[j]);
             d[j]    = __fsub_rn(p[j], s);
-            amax    = fmax_nan(amax, fabsf(d[j]));
         }
+        amax = fmax3_nan(amax, fabsf(d[0]), fabsf(d[1]));
+        amax = fmax3_nan(amax, fabsf(d[2]), fabsf(d[3]));
         const uint32_t q = it * 16 + (lane >> 1);
         *reinterpret_cast<uint2*>(sm + swz(q) + (lane & 1u) * 2) =
             make_uint2(pack_signed_pair(d[0], d[1]), pack_signed_pair(d[2], d[3]));
