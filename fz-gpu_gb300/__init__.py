@@ -458,13 +458,15 @@ class Batch:
 class Server:
     """Request loop with continuous batching under an HBM budget (fz_server_*).
     Requests use host buffers, or device buffers with device=True (FZ_REQUEST_DEVICE);
-    keep them alive until their completion is polled."""
+    keep them alive until their completion is polled.  submit and poll may be called
+    from several threads; a completion goes to whichever thread polls it."""
 
     def __init__(self, hbm_budget, slots, max_n):
+        import threading
         h = C.c_void_p()
         _check("fz_server_create", lib().fz_server_create(int(hbm_budget), int(slots), int(max_n), C.byref(h)))
         self.handle = h
-        self._out = (Completion * 256)()
+        self._tls = threading.local()  # completion buffer per polling thread
 
     def submit(self, rid, direction, src, dst, dst_capacity, n=0, dims=(1, 1, 1), eb=0.0, rel=True,
                mode=MODE_SIDECAR, src_bytes=0, device=False, header=None):
@@ -477,9 +479,12 @@ class Server:
 
     def poll(self):
         """Retire finished requests and admit queued ones; returns [(id, status, bytes)]."""
+        out = getattr(self._tls, "out", None)
+        if out is None:
+            out = self._tls.out = (Completion * 256)()
         cnt = C.c_uint32()
-        _check("fz_server_poll", lib().fz_server_poll(self.handle, self._out, 256, C.byref(cnt)))
-        return [(self._out[i].id, self._out[i].status, self._out[i].bytes) for i in range(cnt.value)]
+        _check("fz_server_poll", lib().fz_server_poll(self.handle, out, 256, C.byref(cnt)))
+        return [(out[i].id, out[i].status, out[i].bytes) for i in range(cnt.value)]
 
     def pending(self):
         q, r, u = C.c_uint32(), C.c_uint32(), C.c_uint64()

@@ -148,3 +148,72 @@ def test_failed_request_does_not_poison_its_slot(fz, synth):
             assert done[1][0] == fz.SUCCESS and done[1][1] == alone.size
             assert np.array_equal(outs[1][: alone.size].cpu().numpy(), alone)
     server.close()
+
+
+def test_submit_and_poll_from_several_threads(fz, synth):
+    """Four host threads submit compress and decompress requests and poll at the same time
+    (fz_server_* may be called from any thread): every request completes exactly once and
+    every result equals the one computed alone."""
+    import threading
+    import time
+    items = _fields(synth)
+    ws = fz.Workspace(max(d.size for d, _, _ in items))
+    alone = [fz.compress_host(d, dims, eb, ws=ws) for d, dims, eb in items]
+    alone_rec = [fz.decompress_host(s, ws=ws) for s in alone]
+    caps = [fz.max_compressed_bytes(d.size, dims) for d, dims, _ in items]
+    hin = [torch.from_numpy(d).pin_memory() for d, _, _ in items]
+    hst = [torch.from_numpy(s.copy()).pin_memory() for s in alone]
+    nthreads = 4
+    outs, reqs = {}, [[] for _ in range(nthreads)]
+    for t in range(nthreads):
+        for i, (d, dims, eb) in enumerate(items):
+            rc, rd = 1000 * t + 2 * i, 1000 * t + 2 * i + 1
+            outs[rc] = torch.empty(caps[i], dtype=torch.uint8).pin_memory()
+            outs[rd] = torch.empty(d.size, dtype=torch.float32).pin_memory()
+            reqs[t].append(dict(rid=rc, direction=fz.COMPRESS, src=hin[i].data_ptr(), dst=outs[rc].data_ptr(),
+                                dst_capacity=caps[i], n=d.size, dims=dims, eb=eb))
+            reqs[t].append(dict(rid=rd, direction=fz.DECOMPRESS, src=hst[i].data_ptr(), dst=outs[rd].data_ptr(),
+                                dst_capacity=4 * d.size, src_bytes=alone[i].size))
+    total = sum(len(r) for r in reqs)
+    server = fz.Server(256 << 20, 4, max(d.size for d, _, _ in items))
+    lock, done, errors = threading.Lock(), [], []
+
+    def worker(t):
+        try:
+            torch.cuda.set_device(0)
+            for r in reqs[t]:
+                server.submit(**r)
+                got = server.poll()
+                with lock:
+                    done.extend(got)
+            deadline = time.monotonic() + 120
+            while True:
+                got = server.poll()
+                with lock:
+                    done.extend(got)
+                    if len(done) >= total:
+                        return
+                if time.monotonic() > deadline:
+                    raise TimeoutError(f"{len(done)} of {total} requests completed")
+        except Exception as ex:  # surfaced below
+            errors.append(ex)
+
+    th = [threading.Thread(target=worker, args=(t,), daemon=True) for t in range(nthreads)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join(timeout=300)
+    assert not errors, errors
+    assert not any(x.is_alive() for x in th)
+    ids = [rid for rid, _, _ in done]
+    assert len(ids) == total and len(set(ids)) == total
+    for rid, st, nb in done:
+        i = (rid % 1000) // 2
+        assert st == fz.SUCCESS, (rid, st)
+        if rid % 2 == 0:
+            assert nb == alone[i].size and np.array_equal(outs[rid][:nb].numpy(), alone[i])
+        else:
+            assert np.array_equal(outs[rid].numpy().view(np.uint32), alone_rec[i].view(np.uint32))
+    assert server.pending() == (0, 0, 0)
+    server.close()
+
