@@ -273,6 +273,11 @@ __device__ __forceinline__ void store4(float* out, uint32_t lin, uint32_t live, 
 // shares with the next window) and the output once.
 constexpr uint32_t kW2 = 960;
 
+// kAl: x % 4 == 0.  Windows start at multiples of 960 columns, so every row's window then
+// starts on a 4-code boundary: a thread's 4 codes are one 8-byte pair of row-buffer words,
+// its 4 outputs one 16-byte store (c1 - c0 is a multiple of 4, so a live thread has all
+// 4 columns), and nothing about alignment or width is decided per row.
+template <bool kAl>
 __global__ void __launch_bounds__(256, 5) k_decompress2d(const DecodeArgs a, uint32_t nwin)
 {
     __shared__ __align__(16) uint32_t rows[16][16 * kSlotWords];  // 16 rows x 16 slots of 64 codes
@@ -297,6 +302,36 @@ __global__ void __launch_bounds__(256, 5) k_decompress2d(const DecodeArgs a, uin
     const bool     live = col < c1;
     const uint32_t q    = tid & 3u;
     uint32_t       acc[4] = {0, 0, 0, 0};
+    if (kAl) {
+        const uint32_t nrows = min(16u, a.y - r0);
+        uint32_t       lin0  = r0 * a.x + c0;  // first code of the window in row r0 + rr
+#pragma unroll 4
+        for (uint32_t rr = 0; rr < 16; ++rr) {
+            if (rr >= nrows) break;  // uniform across the CTA
+            uint32_t d[4] = {0, 0, 0, 0};
+            if (live) {
+                const uint32_t i = (lin0 & 63u) + 4 * tid;
+                const uint2    v = *reinterpret_cast<const uint2*>(rows[rr] + (i >> 6) * kSlotWords + ((i & 63u) >> 1));
+                sm_decode2(v.x, d[0], d[1]);
+                sm_decode2(v.y, d[2], d[3]);
+            }
+            d[1] += d[0], d[2] += d[1], d[3] += d[2];
+            uint32_t v = d[3];
+            uint32_t u = __shfl_up_sync(kFull, v, 1);
+            if (q >= 1) v += u;
+            u = __shfl_up_sync(kFull, v, 2);
+            if (q >= 2) v += u;
+            const uint32_t ex = v - d[3];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[j] += d[j] + ex;
+            if (live)
+                *reinterpret_cast<float4*>(a.out + lin0 + 4 * tid) =
+                    make_float4((float)(int32_t)acc[0] * a.ebx2, (float)(int32_t)acc[1] * a.ebx2,
+                                (float)(int32_t)acc[2] * a.ebx2, (float)(int32_t)acc[3] * a.ebx2);
+            lin0 += a.x;
+        }
+        return;
+    }
 #pragma unroll 4
     for (uint32_t rr = 0; rr < 16; ++rr) {
         const uint32_t row = r0 + rr;
@@ -539,7 +574,9 @@ cudaError_t launch_decompress_fused(const DecodeArgs& a, cudaStream_t s)
     const int nd = (a.z == 1 && a.y == 1) ? 1 : (a.z == 1 ? 2 : 3);
     if (nd == 2) {
         const uint32_t nwin = (uint32_t)cdiv(a.x, kW2);
-        k_decompress2d<<<(uint32_t)(nwin * cdiv(a.y, 16)), 256, 0, s>>>(a, nwin);
+        const uint32_t ctas = (uint32_t)(nwin * cdiv(a.y, 16));
+        if (a.x % 4 == 0) k_decompress2d<true><<<ctas, 256, 0, s>>>(a, nwin);
+        else k_decompress2d<false><<<ctas, 256, 0, s>>>(a, nwin);
         return cudaGetLastError();
     }
     if (nd == 3) {
