@@ -308,24 +308,41 @@ __device__ __forceinline__ void block2d_u(const float* __restrict__ in, const Ge
 #pragma unroll 4
     for (uint32_t it = 0; it < 16; ++it) {
         const float4 vn = it < 15 ? ldg4(in + e0 + 128) : v;
-        const Pos4   P  = pos4(g, row0, col0);
         const float  c[4] = {v.x, v.y, v.z, v.w};
-        float        t[4];
+        // the lane's 4 elements cross a row end only where a row boundary falls inside its
+        // group (rare): otherwise they share one row and the tile tests are made once
+        const bool wrap = col0 + 3 >= g.x;
+        float      t[4];
+        if (!wrap) {
+            const bool nz = (row0 & 15u) != 0;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const float nq = (P.row[j] & 15u) ? pq(__ldg(in + (e0 + j - g.x)), r) : 0.0f;
-            t[j]           = __fsub_rn(pq(c[j], r), nq);
+            for (int j = 0; j < 4; ++j) {
+                const float nq = nz ? pq(__ldg(in + (e0 + j - g.x)), r) : 0.0f;
+                t[j]           = __fsub_rn(pq(c[j], r), nq);
+            }
+        } else {
+            const Pos4 P = pos4(g, row0, col0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float nq = (P.row[j] & 15u) ? pq(__ldg(in + (e0 + j - g.x)), r) : 0.0f;
+                t[j]           = __fsub_rn(pq(c[j], r), nq);
+            }
         }
         const float rot = __shfl_sync(kFull, t[3], prev);  // lane 0: lane 31's, for the next group row
         const float tw  = lane ? rot : carry;
         carry           = rot;
         float d[4];
+        if (!wrap) {
+            const uint32_t k = (0u - col0) & 15u;  // element k starts a tile row (when k < 4)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const float w = (P.col[j] & 15u) ? (j ? t[j - 1] : tw) : 0.0f;
-            d[j]          = __fsub_rn(t[j], w);
-            amax          = fmax_nan(amax, fabsf(d[j]));
+            for (int j = 0; j < 4; ++j) d[j] = __fsub_rn(t[j], (uint32_t)j == k ? 0.0f : (j ? t[j - 1] : tw));
+        } else {
+            const Pos4 P = pos4(g, row0, col0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) d[j] = __fsub_rn(t[j], (P.col[j] & 15u) ? (j ? t[j - 1] : tw) : 0.0f);
         }
+        amax = fmax3_nan(amax, fabsf(d[0]), fabsf(d[1]));
+        amax = fmax3_nan(amax, fabsf(d[2]), fabsf(d[3]));
         *reinterpret_cast<uint2*>(sm + it * 64 + so.x0) =
             make_uint2(pack_signed_pair(d[0], d[1]), pack_signed_pair(d[2], d[3]));
         so.next();
