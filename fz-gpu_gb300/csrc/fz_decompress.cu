@@ -504,6 +504,25 @@ static cudaError_t allow_decompress3d_smem()
 // their sign; the others take it from the sidecar sign bits (or are non-negative).
 constexpr int kDecode1dWarps = 4;
 
+// Lane-local inclusive prefix of the lane's 64 deltas into shared memory (swizzled so the
+// 32 lanes hit 32 banks); codes at i%4 == 0 carry their sign, the others take it from the
+// sidecar words s0, s1.  kCheck: only the first lim deltas count (the run ends past x*y*z).
+template <bool kCheck>
+__device__ __forceinline__ uint32_t run1d(const uint32_t (&w)[32], uint32_t s0, uint32_t s1, uint32_t lim,
+                                          uint32_t lane, uint32_t* sm)
+{
+    uint32_t acc = 0;
+#pragma unroll
+    for (int j = 0; j < 64; ++j) {
+        const uint32_t c   = (j & 1) ? (w[j >> 1] >> 16) : (w[j >> 1] & 0xFFFFu);
+        const uint32_t sgn = ((j < 32 ? s0 >> j : s1 >> (j - 32)) & 1u);
+        const uint32_t d   = (j & 3) == 0 ? sm_decode(c) : (sgn ? 0u - c : c);
+        acc += (!kCheck || (uint32_t)j < lim) ? d : 0u;
+        sm[(j ^ lane) + 64 * lane] = acc;
+    }
+    return acc;
+}
+
 __global__ void __launch_bounds__(kDecode1dWarps * 32) k_decompress1d(const DecodeArgs a)
 {
     __shared__ __align__(16) uint32_t smem[kDecode1dWarps][2048];
@@ -530,15 +549,9 @@ __global__ void __launch_bounds__(kDecode1dWarps * 32) k_decompress1d(const Deco
         s0 = __ldg(sb + (e0 >> 5));
         s1 = (e0 + 32 < a.n) ? __ldg(sb + (e0 >> 5) + 1) : 0u;
     }
-    uint32_t acc = 0;
-#pragma unroll
-    for (int j = 0; j < 64; ++j) {
-        const uint32_t c   = (j & 1) ? (w[j >> 1] >> 16) : (w[j >> 1] & 0xFFFFu);
-        const uint32_t sgn = ((j < 32 ? s0 >> j : s1 >> (j - 32)) & 1u);
-        const uint32_t d   = (j & 3) == 0 ? sm_decode(c) : (sgn ? 0u - c : c);
-        acc += (e0 + j < a.nl) ? d : 0u;
-        sm[(j ^ lane) + 64 * lane] = acc;  // lane-local run, swizzled so the 32 lanes hit 32 banks
-    }
+    // elements of this lane's run inside x*y*z (all 64 except in the last block)
+    const uint32_t lim = a.nl > e0 ? a.nl - e0 : 0u;
+    const uint32_t acc = lim >= 64 ? run1d<false>(w, s0, s1, lim, lane, sm) : run1d<true>(w, s0, s1, lim, lane, sm);
     // carry across the 4 lanes of each 256-element block
     uint32_t v = acc, u = __shfl_up_sync(kFull, v, 1);
     if (lane & 3u) v += u;
