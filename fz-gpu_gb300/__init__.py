@@ -30,6 +30,7 @@ OUT_OF_SPACE = 0x0202
 TIMEOUT = 0x0203
 NONFINITE_INPUT = 0x0205
 MODE_COMPAT, MODE_SIDECAR = 0, 1
+FLAG_CODE_OVERFLOW, FLAG_FAILED = 0x1, 0x2  # fz_header.flags
 EB_ABS, EB_REL = 0, 1
 HEADER_BYTES = 64
 BLOCK_CODES = 2048
@@ -226,7 +227,9 @@ class Workspace:
         """Status of a look-back that waits on a tile nothing publishes (FZ_TIMEOUT)."""
         return lib().fz_selftest_wait_timeout(self.handle, _stream_handle(stream))
 
-    KERNELS = ("k_range", "k_compress", "k_offsets", "k_decode", "k_recon", "k_compact")
+    # timing kinds of fz_workspace_kernel_time, by the kernels they time: k_encode<ND> and
+    # k_decompress{1,2,3}d are templated / specialised per dimensionality
+    KERNELS = ("k_range", "k_encode", "k_offsets", "k_decompress", "k_recon", "k_compact")
 
     def enable_timing(self, capacity):
         _check("fz_workspace_enable_timing", lib().fz_workspace_enable_timing(self.handle, int(capacity)))

@@ -48,10 +48,12 @@ Layout make_layout(uint64_t n, uint32_t x, uint32_t y, uint32_t z, uint32_t mode
 }  // namespace fz
 
 namespace {
-
 constexpr uint64_t kMaxN = 1ull << 31;
+}  // namespace
 
-fz_status map_err(cudaError_t e, fz_status dflt = FZ_FAIL_GPU_ILLEGAL_ACCESS)
+namespace fz {
+
+fz_status map_err(cudaError_t e, fz_status dflt)
 {
     if (e == cudaSuccess) return FZ_SUCCESS;
     if (e == cudaErrorMemoryAllocation) return FZ_FAIL_GPU_OUT_OF_MEMORY;
@@ -59,17 +61,23 @@ fz_status map_err(cudaError_t e, fz_status dflt = FZ_FAIL_GPU_ILLEGAL_ACCESS)
     return dflt;
 }
 
+bool dims_fit(uint64_t n, uint32_t x, uint32_t y, uint32_t z)
+{
+    if (n == 0 || n > kMaxN || x == 0 || y == 0 || z == 0) return false;
+    const uint64_t xy = (uint64_t)x * y;  // < 2^64: both factors < 2^32
+    if (xy > n) return false;
+    return (uint64_t)z <= n / xy;         // xy * z <= n, without forming the product
+}
+
+}  // namespace fz
+
+namespace {
+
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 int ndim_of(fz_dims d) { return (d.z == 1 && d.y == 1) ? 1 : (d.z == 1 ? 2 : 3); }
 
-fz_status check_dims(uint64_t n, fz_dims d)
-{
-    if (n == 0 || n > kMaxN || d.x == 0 || d.y == 0 || d.z == 0) return FZ_INVALID_ARG;
-    const uint64_t nl = (uint64_t)d.x * d.y * d.z;
-    if (nl > n) return FZ_INVALID_ARG;
-    return FZ_SUCCESS;
-}
+fz_status check_dims(uint64_t n, fz_dims d) { return dims_fit(n, d.x, d.y, d.z) ? FZ_SUCCESS : FZ_INVALID_ARG; }
 
 uint64_t max_stream(const Layout& L) { return L.off_b + 16ull * kChunks * L.nb; }
 
@@ -119,7 +127,7 @@ fz_status readback(fz_workspace* ws, const void* d_stream, cudaStream_t s, fz_he
 fz_status validate_header(const fz_header* h, uint64_t stream_bytes, Layout* out)
 {
     if (h->magic != FZ_MAGIC || h->version != FZ_FORMAT_VERSION) return FZ_CORRUPT_STREAM;
-    if (h->mode > 1) return FZ_CORRUPT_STREAM;
+    if (h->mode > 1 || (h->flags & FZ_FLAG_FAILED)) return FZ_CORRUPT_STREAM;
     fz_dims d{h->x, h->y, h->z};
     if (check_dims(h->n, d) != FZ_SUCCESS || ndim_of(d) != h->ndim) return FZ_CORRUPT_STREAM;
     Layout L = make_layout(h->n, h->x, h->y, h->z, h->mode);
@@ -378,7 +386,7 @@ fz_status fz::compress_impl(fz_workspace* ws, const float* d_in, uint64_t n, fz_
     cudaError_t e = cudaSuccess;
     if (eb_mode == FZ_EB_REL) {
         KernelTimer t(ws, s, 0);
-        e        = launch_range(d_in, L.n, ws->mm, ws->status, s);
+        e        = launch_range(d_in, L.n, ws->mm, ws->status, ws->ovfw, s);
         a.mm     = ws->mm;
         a.eb_rel = eb;
     } else {

@@ -19,6 +19,7 @@
 // are exactly the 8 bitmap words of the block) and writes its non-zero chunks with
 // 128-bit stores.
 #include <algorithm>
+#include <atomic>
 
 #include "fz_internal.h"
 
@@ -645,9 +646,10 @@ constexpr int kRangeUnroll = 8;
 // (coalesced across the CTA); the grid covers the field in one batch per thread, so the
 // block scheduler keeps every SM streaming until the last CTAs.  NaN/Inf raise
 // kStatusNonfinite: the running min and max propagate NaN (min.NaN / max.NaN), so one
-// test of each thread's final pair finds any NaN, -Inf or +Inf it has seen.
+// test of each thread's final pair finds any NaN, -Inf or +Inf it has seen; the bit also
+// goes to `callw` (a per-call word the header writer reads and resets), when given.
 __global__ void __launch_bounds__(256) k_range(const float* __restrict__ in, uint32_t n, uint32_t* mm,
-                                               uint32_t* status)
+                                               uint32_t* status, uint32_t* callw)
 {
     __shared__ uint32_t smn[8], smx[8], snf[8];
     float          mn = INFINITY, mx = -INFINITY;
@@ -691,7 +693,10 @@ __global__ void __launch_bounds__(256) k_range(const float* __restrict__ in, uin
         if (lane == 0) {
             atomicMin(mm, a);
             atomicMax(mm + 1, c);
-            if (f) atomicOr(status, kStatusNonfinite);
+            if (f) {
+                atomicOr(status, kStatusNonfinite);
+                if (callw) atomicOr(callw, kStatusNonfinite);
+            }
         }
     }
 }
@@ -716,13 +721,13 @@ __device__ EbInfo eb_from_range(float vmin, float vmax, double rel)
 // ------------------------------------------------------------ compress --
 constexpr int kCompressWarps = 8;
 
-// Stream header (struct fz_header, include/fz.h), written by the last tile once its
-// inclusive prefix -- the stream's chunk count -- is known.
-__device__ void write_header(const CompressArgs& a, const EbInfo& e, uint32_t ovf, uint32_t nnz)
+// Stream header (struct fz_header, include/fz.h), written once the stream's chunk count is
+// known.  flags: FZ_FLAG_CODE_OVERFLOW (1) and FZ_FLAG_FAILED (2).
+__device__ void write_header(const CompressArgs& a, const EbInfo& e, uint32_t flags, uint32_t nnz)
 {
     uint8_t* h = a.out;
     *reinterpret_cast<uint4*>(h + 0)  = make_uint4(0x31475A46u, 1u | (a.mode << 16) | (a.ndim << 24), a.x, a.y);
-    *reinterpret_cast<uint4*>(h + 16) = make_uint4(a.z, ovf ? 1u : 0u, a.n, 0u);
+    *reinterpret_cast<uint4*>(h + 16) = make_uint4(a.z, flags, a.n, 0u);
     const unsigned long long eb = __double_as_longlong(e.eb_abs);
     *reinterpret_cast<uint4*>(h + 32) = make_uint4((uint32_t)eb, (uint32_t)(eb >> 32), __float_as_uint(e.ebx2_r),
                                                    __float_as_uint(e.ebx2));
@@ -922,7 +927,7 @@ __global__ void __launch_bounds__(kCompressWarps * 32, 3) k_compress(const Compr
                 }
                 if (lane < kCompressWarps) s_pre[lane] = excl + inc - c;
                 if (lane == 0 && prev_ct == nct - 1) {
-                    write_header(a, eb, tov | povf, excl + tot);
+                    write_header(a, eb, (tov | povf) ? 1u : 0u, excl + tot);
                     if (a.boff) {
                         // the total closes the offset table; zero its 16-byte pad
                         a.boff[a.nb] = excl + tot;
@@ -953,6 +958,21 @@ __global__ void __launch_bounds__(kCompressWarps * 32, 3) k_compress(const Compr
 #pragma unroll
         for (int i = 0; i < 8; ++i) bm_prev[i] = bm[i];
         prev_ct = ct;
+    }
+    // The last CTA to leave marks the header when this call raised a status bit (non-finite
+    // input, a wait that gave up), so a caller that reads no status still sees the failure
+    // in the stream; it also resets the exit counter for the next call.
+    if (a.fin) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();  // this CTA's stream writes (the header, if it wrote it) come first
+            if (atomicAdd(a.fin, 1u) == gridDim.x - 1) {
+                __threadfence();
+                if (__ldcg(a.status) & (kStatusTimeout | kStatusNonfinite))
+                    atomicOr(reinterpret_cast<uint32_t*>(a.out + 20), FZ_FLAG_FAILED);
+                *a.fin = 0;
+            }
+        }
     }
 }
 
@@ -1089,7 +1109,9 @@ __global__ void __launch_bounds__(256) k_compact(const CompressArgs a, const uin
     for (uint32_t i = tid; i < nsup; i += blockDim.x) supers[i] = 0;
     if (tid == 0) {
         const EbInfo eb = a.mm ? eb_from_range(ord2f(__ldcg(a.mm)), ord2f(__ldcg(a.mm + 1)), a.eb_rel) : a.ebh;
-        write_header(a, eb, __ldcg(ovfw), total);
+        // ovfw: bit 0 some code overflowed (k_encode), kStatusNonfinite (k_range) -- this call's own bits
+        const uint32_t cw = __ldcg(ovfw);
+        write_header(a, eb, ((cw & 1u) ? 1u : 0u) | ((cw & kStatusNonfinite) ? 2u : 0u), total);
         if (a.boff) {
             // the total closes the offset table; zero its 16-byte pad
             a.boff[a.nb] = total;
@@ -1126,23 +1148,28 @@ cudaError_t launch_wait_selftest(const uint64_t* state, const uint32_t* epoch, u
     return cudaGetLastError();
 }
 
-// Resident CTAs per SM of a kernel, and the SM count, queried once per process.
+// Resident CTAs of a kernel on the current device (SM count x CTAs per SM), after the
+// device's opt-in to more than 48 KiB of dynamic shared memory where the kernel needs it;
+// 0 when a query fails.
 template <typename K>
 static uint32_t resident_ctas(K kernel, int threads, int dyn_smem = 0)
 {
     int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (dyn_smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, dyn_smem);
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (dyn_smem > 48 * 1024 &&
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem) != cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, dyn_smem) != cudaSuccess) return 0;
     return (uint32_t)std::max(1, sms * std::max(per_sm, 1));
 }
 
-cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* status, cudaStream_t s)
+cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* status, uint32_t* callw,
+                         cudaStream_t s)
 {
     const uint64_t want = cdiv(n / 4, 256ull * kRangeUnroll);  // n < 2^31: at most 2^18 CTAs
     const uint32_t ctas = (uint32_t)std::max<uint64_t>(1, want);
-    k_range<<<ctas, 256, 0, s>>>(in, n, mm, status);
+    k_range<<<ctas, 256, 0, s>>>(in, n, mm, status, callw);
     return cudaGetLastError();
 }
 
@@ -1166,15 +1193,34 @@ cudaError_t launch_compact(const CompressArgs& a, const uint4* slots, const uint
     return cudaGetLastError();
 }
 
+// One resident wave of k_compress<ND> on the current device.  The 64 KiB of dynamic shared
+// memory needs a per-device opt-in, and the wave depends on the device's SM count, so
+// both are done and cached per device (device ordinals below 64; others are computed on
+// every call).
+static uint32_t compress_wave(int nd)
+{
+    constexpr int                       kSmem = 2 * kCompressWarps * kBlockWords * 4;  // two tile buffers
+    static std::atomic<uint32_t>        cache[64][3];
+    int                                 dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    std::atomic<uint32_t>* slot = (dev >= 0 && dev < 64) ? &cache[dev][nd - 1] : nullptr;
+    uint32_t               w    = slot ? slot->load(std::memory_order_acquire) : 0u;
+    if (w) return w;
+    w = nd == 1 ? resident_ctas(k_compress<1>, kCompressWarps * 32, kSmem)
+        : nd == 2 ? resident_ctas(k_compress<2>, kCompressWarps * 32, kSmem)
+                  : resident_ctas(k_compress<3>, kCompressWarps * 32, kSmem);
+    if (slot) slot->store(w, std::memory_order_release);
+    return w;
+}
+
 cudaError_t launch_compress(const CompressArgs& a, cudaStream_t s)
 {
     // persistent: min(tiles, one resident wave) CTAs; a tile is 8 shuffle blocks
-    constexpr int         kSmem   = 2 * kCompressWarps * kBlockWords * 4;  // two tile buffers
-    static const uint32_t wave[3] = {resident_ctas(k_compress<1>, kCompressWarps * 32, kSmem),
-                                     resident_ctas(k_compress<2>, kCompressWarps * 32, kSmem),
-                                     resident_ctas(k_compress<3>, kCompressWarps * 32, kSmem)};
+    constexpr int  kSmem = 2 * kCompressWarps * kBlockWords * 4;  // two tile buffers
+    const uint32_t wave  = compress_wave((int)a.ndim);
+    if (!wave) return cudaErrorInvalidDevice;
     const uint32_t nct  = (uint32_t)cdiv(a.ntiles, kCompressWarps);
-    const uint32_t ctas = std::min(nct, wave[a.ndim - 1]);
+    const uint32_t ctas = std::min(nct, wave);
     switch (a.ndim) {
     case 1: k_compress<1><<<ctas, kCompressWarps * 32, kSmem, s>>>(a); break;
     case 2: k_compress<2><<<ctas, kCompressWarps * 32, kSmem, s>>>(a); break;

@@ -4,12 +4,21 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/fz.h"
 #include "fz_device.cuh"
 
 namespace fz {
 
 __host__ __device__ inline uint64_t cdiv(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
 __host__ __device__ inline uint64_t pad16(uint64_t a) { return (a + 15) & ~uint64_t(15); }
+
+// A CUDA error as the status the C ABI reports (allocation and device-presence errors
+// keep their own codes; everything else becomes `dflt`).
+fz_status map_err(cudaError_t e, fz_status dflt = FZ_FAIL_GPU_ILLEGAL_ACCESS);
+// x*y*z <= n without wrapping (each product is checked against n before the next one),
+// every dimension at least 1 and 0 < n <= 2^31.  Every path that sizes a launch or a
+// stream from dims (arguments or a stream header) goes through this check.
+bool dims_fit(uint64_t n, uint32_t x, uint32_t y, uint32_t z);
 
 // Geometry of one field and its stream.
 struct Layout {
@@ -41,6 +50,7 @@ struct CompressArgs {
     uint32_t*    epoch;  // device epoch word (advanced by the kernel's last ticket fetch)
     uint32_t*    boff;   // block offset table in the stream's sidecar, or null
     uint32_t*    mirror; // k_compact: 64-byte header + status word copied here, or null
+    uint32_t*    fin;    // k_compress: CTA exit counter (zero on entry, left zero), or null
 };
 
 struct DecodeArgs {
@@ -63,7 +73,9 @@ struct ReconArgs {
 };
 
 // launchers (return the launch error)
-cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* status, cudaStream_t s);
+// callw: nullable per-call word that also receives kStatusNonfinite
+cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* status, uint32_t* callw,
+                         cudaStream_t s);
 cudaError_t launch_compress(const CompressArgs& a, cudaStream_t s);  // fused, single launch
 // two launches with per-block slots in a scratch of 4 KiB per shuffle block (workspace path);
 // supers: chunk counts per 512 blocks (zero on entry, left zero), done: a zero word

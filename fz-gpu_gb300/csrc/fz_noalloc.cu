@@ -27,7 +27,7 @@ namespace {
 // Scan tiles of the largest field: ceil((n/2048 + 1) / 8), plus slack.
 constexpr uint32_t kNoallocTiles = (uint32_t)((FZ_NOALLOC_MAX_ELEMS / kBlockCodes + 1) / 8 + 2);
 // u64 words: tile states, then 2 words of control: [mm_min, mm_max, status, ticket],
-// then 1 word [epoch, pad].
+// then 1 word [epoch, CTA exit counter].
 constexpr uint32_t kNoallocWords = kNoallocTiles + 3;
 static_assert(kNoallocWords * 8 <= FZ_NOALLOC_SCRATCH_BYTES, "scratch size");
 
@@ -50,7 +50,7 @@ fz_status scratch_for_current_device(uint64_t** out)
     if (!g_addr[dev]) {
         void*       p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) return FZ_FAIL_GPU_ILLEGAL_ACCESS;
+        if (e != cudaSuccess || !p) return e != cudaSuccess ? map_err(e) : FZ_FAIL_GPU_ILLEGAL_ACCESS;
         g_addr[dev] = p;
     }
     *out = static_cast<uint64_t*>(g_addr[dev]);
@@ -67,7 +67,7 @@ extern "C" fz_status fz_compress_noalloc(const float* d_in, uint64_t n, fz_dims 
     if (n == 0 || n > FZ_NOALLOC_MAX_ELEMS) return FZ_INVALID_ARG;
     if (!d_in || !d_out || (reinterpret_cast<uintptr_t>(d_in) & 15u) || (reinterpret_cast<uintptr_t>(d_out) & 15u))
         return FZ_INVALID_ARG;
-    if (dims.x == 0 || dims.y == 0 || dims.z == 0 || (uint64_t)dims.x * dims.y * dims.z > n) return FZ_INVALID_ARG;
+    if (!dims_fit(n, dims.x, dims.y, dims.z)) return FZ_INVALID_ARG;
     if (!(eb > 0) || !std::isfinite(eb)) return FZ_INVALID_ARG;
     if ((eb_mode != FZ_EB_ABS && eb_mode != FZ_EB_REL) || (mode != FZ_MODE_COMPAT && mode != FZ_MODE_SIDECAR))
         return FZ_INVALID_ARG;
@@ -79,12 +79,15 @@ extern "C" fz_status fz_compress_noalloc(const float* d_in, uint64_t n, fz_dims 
     if (st != FZ_SUCCESS) return st;
     uint32_t* ctl   = reinterpret_cast<uint32_t*>(scratch + kNoallocTiles);  // mm_min, mm_max, status, ticket
     uint32_t* epoch = reinterpret_cast<uint32_t*>(scratch + kNoallocTiles + 2);
+    uint32_t* fin   = epoch + 1;
 
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    // the previous call's contents: reset the range to "empty", the status and ticket to 0
+    // the previous call's contents: reset the range to "empty", the status, ticket and exit
+    // counter to 0 (the epoch only moves forward and is kept)
     cudaError_t e = cudaMemsetAsync(ctl, 0xFF, 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctl + 1, 0, 12, s);
-    if (e != cudaSuccess) return FZ_FAIL_GPU_ILLEGAL_ACCESS;
+    if (e == cudaSuccess) e = cudaMemsetAsync(fin, 0, 4, s);
+    if (e != cudaSuccess) return map_err(e);
 
     CompressArgs a{};
     a.in = d_in, a.out = static_cast<uint8_t*>(d_out);
@@ -96,8 +99,9 @@ extern "C" fz_status fz_compress_noalloc(const float* d_in, uint64_t n, fz_dims 
     a.off_a = L.off_a, a.off_c = L.off_c, a.off_b = L.off_b, a.off_sign = L.off_sign, a.off_boff = L.off_boff;
     a.state = scratch, a.ticket = ctl + 3, a.status = ctl + 2, a.epoch = epoch;
     a.boff  = mode == FZ_MODE_SIDECAR ? reinterpret_cast<uint32_t*>(a.out + L.off_boff) : nullptr;
+    a.fin   = fin;
     if (eb_mode == FZ_EB_REL) {
-        e        = launch_range(d_in, L.n, ctl, ctl + 2, s);
+        e        = launch_range(d_in, L.n, ctl, ctl + 2, nullptr, s);
         a.mm     = ctl;
         a.eb_rel = eb;
     } else {
@@ -109,7 +113,10 @@ extern "C" fz_status fz_compress_noalloc(const float* d_in, uint64_t n, fz_dims 
         a.ebh.range = a.ebh.vmin = a.ebh.vmax = 0.0f;
     }
     if (e == cudaSuccess) e = launch_compress(a, s);
-    if (e != cudaSuccess) return FZ_FAIL_GPU_ILLEGAL_ACCESS;
+    if (e != cudaSuccess) return map_err(e);
+    // Without the readback the call returns at once; a failure found on the device
+    // (non-finite input with a relative bound, a wait that gave up) is then carried by the
+    // stream itself: its header gets FZ_FLAG_FAILED, which every reader rejects.
     if (!out_bytes) return FZ_SUCCESS;
     // optional size readback into pageable host memory (synchronous)
     fz_header h;
@@ -117,7 +124,7 @@ extern "C" fz_status fz_compress_noalloc(const float* d_in, uint64_t n, fz_dims 
     e = cudaMemcpyAsync(&h, d_out, sizeof(h), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&status, ctl + 2, 4, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return FZ_FAIL_GPU_MEMCPY;
+    if (e != cudaSuccess) return map_err(e, FZ_FAIL_GPU_MEMCPY);
     *out_bytes = L.off_b + 16ull * h.nnz;
     if (status & kStatusTimeout) return FZ_TIMEOUT;
     if (status & kStatusNonfinite) return FZ_NONFINITE_INPUT;

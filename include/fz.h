@@ -71,6 +71,11 @@ typedef enum fz_status {
 /* some delta did not fit its code field (|d| >= 32768 signed, >= 65536 for 1D unsigned
    positions, or non-finite): the stream does not meet the error bound there */
 #define FZ_FLAG_CODE_OVERFLOW 0x1u
+/* the compressing kernels reported a failure (NaN/Inf in a relative-eb input, or a
+   bounded device-side wait that gave up): the stream is not valid, and every entry point
+   that reads a header rejects it with FZ_CORRUPT_STREAM.  Lets a caller that skips the
+   size readback (out_bytes NULL) still see the failure in the stream itself. */
+#define FZ_FLAG_FAILED        0x2u
 
 typedef enum fz_mode {
     /* Sections A+B only: the reference's exact compressed content. Not invertible
@@ -164,7 +169,9 @@ fz_status fz_selftest_wait_timeout(fz_workspace* ws, fz_stream_t stream);
 /* ------------------------------------------------ full pipeline, device -- */
 /* Compress d_in[0..n) (dims describe the first x*y*z elements; n may exceed it as
    in fz.cu:117-118) into d_out.  Replaces runSzs (fz.cu:113-224) minus file I/O.
-   out_bytes: host, nullable, syncs -- the stream's total size. */
+   out_bytes: host, nullable, syncs -- the stream's total size.  Without it, a failure
+   found on the device (NaN/Inf in a relative-eb input) marks the header with
+   FZ_FLAG_FAILED and stays readable through fz_workspace_status. */
 fz_status fz_compress(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims dims,
                       double eb, fz_eb_mode eb_mode, fz_mode mode, void* d_out,
                       uint64_t out_capacity, uint64_t* out_bytes, fz_stream_t stream);
@@ -187,7 +194,11 @@ fz_status fz_decompress(fz_workspace* ws, const void* d_stream, uint64_t stream_
    FZ_INVALID_ARG before anything is launched.  The first call on a device looks up the
    array's device address (cudaGetSymbolAddress), so make that first call before any
    stream capture.  All calls share the array: calls whose GPU work overlaps race, so
-   serialise them (one stream).  No counterpart in the reference. */
+   serialise them (one stream).  out_bytes (host, nullable) reads the size back and
+   synchronises the stream; with it NULL the call returns without waiting, and a failure
+   found on the device (NaN/Inf in a relative-eb input, a wait that gave up) marks the
+   stream's header with FZ_FLAG_FAILED, so fz_stream_bytes and fz_decompress reject it
+   with FZ_CORRUPT_STREAM.  No counterpart in the reference. */
 #define FZ_NOALLOC_MAX_ELEMS     (1ull << 26)
 #define FZ_NOALLOC_SCRATCH_BYTES 33280u
 fz_status fz_compress_noalloc(const float* d_in, uint64_t n, fz_dims dims, double eb,

@@ -251,17 +251,64 @@ void fzo_bitshuffle_flag(const uint16_t* codes, uint64_t n, uint32_t* S, uint32_
 /* cub::DeviceScan::ExclusiveSum over M = 32*ceil(n/256) flags, total = P[M-1] + F[M-1]
    written to P[M] (fz.cu:187-201), then encodeDebug's intended compaction: chunk t with
    P[t+1] != P[t] is copied to out[16*P[t]] (fz.cu:49-59). */
+/* Block-wise parallel form: every thread counts the flags of its contiguous range, one
+   thread turns the counts into exclusive range offsets, then every thread writes its
+   prefix sums and copies its flagged chunks from its range's offset on.  The result is
+   the serial scan's, whatever the thread count. */
 uint64_t fzo_scan_encode(const uint32_t* S, const uint32_t* F, uint64_t n, uint32_t* P,
                          uint8_t* out)
 {
-    uint64_t m   = 32 * cdiv(n, 256);
-    uint64_t acc = 0;
-    for (uint64_t t = 0; t < m; t++) {
-        if (P) P[t] = (uint32_t)acc;
-        if (F[t] && out) memcpy(out + 16 * acc, (const uint8_t*)S + 16 * t, 16);
-        acc += F[t] != 0;
+    uint64_t  m     = 32 * cdiv(n, 256);
+    int       nt    = fzo_threads();
+    uint64_t* part  = (uint64_t*)calloc((size_t)nt + 1, sizeof(uint64_t));
+    uint64_t  total = 0;
+#pragma omp parallel num_threads(nt)
+    {
+#ifdef _OPENMP
+        int tid = omp_get_thread_num(), th = omp_get_num_threads();
+#else
+        int tid = 0, th = 1;
+#endif
+        uint64_t lo = m * (uint64_t)tid / (uint64_t)th, hi = m * (uint64_t)(tid + 1) / (uint64_t)th;
+        uint64_t c  = 0;
+        for (uint64_t t = lo; t < hi; t++) c += F[t] != 0;
+        part[tid + 1] = c;
+#pragma omp barrier
+#pragma omp single
+        {
+            for (int k = 1; k <= th; k++) part[k] += part[k - 1];
+            total = part[th];
+        }
+        uint64_t acc = part[tid];
+        for (uint64_t t = lo; t < hi; t++) {
+            if (P) P[t] = (uint32_t)acc;
+            if (F[t] && out) memcpy(out + 16 * acc, (const uint8_t*)S + 16 * t, 16);
+            acc += F[t] != 0;
+        }
     }
-    if (P) P[m] = (uint32_t)acc;
+    free(part);
+    if (P) P[m] = (uint32_t)total;
+    return total;
+}
+
+/* Chunk offset of every shuffle block (boff[b] = flagged chunks of blocks 0..b-1, the
+   exclusive scan of fz.cu:187-192 at block granularity) from the bitmap: per-block counts
+   in parallel, then their prefix.  Returns the total. */
+static uint64_t block_offsets(const uint32_t* B, uint64_t nb, uint64_t* boff)
+{
+#pragma omp parallel for schedule(static)
+    for (uint64_t b = 0; b < nb; b++) {
+        uint64_t c = 0;
+        for (int k = 0; k < 8; k++) c += (uint64_t)__builtin_popcount(B[b * 8 + k]);
+        boff[b] = c;
+    }
+    uint64_t acc = 0;
+    for (uint64_t b = 0; b < nb; b++) {
+        uint64_t c = boff[b];
+        boff[b]    = acc;
+        acc += c;
+    }
+    boff[nb] = acc;
     return acc;
 }
 
@@ -296,8 +343,10 @@ uint64_t fzo_compress(const float* data, uint64_t n, uint32_t x, uint32_t y, uin
     double eb_abs = eb;
     if (eb_mode == 1) {
         float mn, mx;
-        for (uint64_t i = 0; i < n; i++)
-            if (!isfinite(data[i])) return 0; /* relative eb of a non-finite field */
+        int   bad = 0;
+#pragma omp parallel for reduction(| : bad) schedule(static)
+        for (uint64_t i = 0; i < n; i++) bad |= !isfinite(data[i]);
+        if (bad) return 0; /* relative eb of a non-finite field */
         fzo_value_range(data, n, &mn, &mx);
         range  = mx - mn;
         eb_abs = eb * range; /* fz.cu:149: eb * range, double * float */
@@ -328,18 +377,22 @@ uint64_t fzo_compress(const float* data, uint64_t n, uint32_t x, uint32_t y, uin
         memcpy(out + off_c, codes + nb * BLOCK_CODES, tail * 2);
         uint64_t q = off_c + pad16(2 * tail);
         if (nd == 1) {
+            /* one sign bit per element, bit i%8 of byte i/8 */
             uint8_t* sb = out + q;
-            for (uint64_t i = 0; i < n; i++)
-                if (sg[i]) sb[i >> 3] |= (uint8_t)(1u << (i & 7));
+            uint64_t nbytes = cdiv(n, 8);
+#pragma omp parallel for schedule(static)
+            for (uint64_t k = 0; k < nbytes; k++) {
+                uint8_t v = 0;
+                for (uint64_t i = 8 * k; i < 8 * k + 8 && i < n; i++) v |= (uint8_t)((sg[i] ? 1u : 0u) << (i & 7));
+                sb[k] = v;
+            }
             q += pad16(4 * cdiv(n, 32));
         }
         /* boff[b] = chunks of blocks 0..b-1, boff[nb] = nnz */
-        uint32_t acc = 0;
-        for (uint64_t b = 0; b <= nb; b++) {
-            put32(out + q + 4 * b, acc);
-            if (b < nb)
-                for (int k = 0; k < 8; k++) acc += (uint32_t)__builtin_popcount(B[b * 8 + k]);
-        }
+        uint64_t* boff = (uint64_t*)malloc((nb + 1) * 8);
+        block_offsets(B, nb, boff);
+        for (uint64_t b = 0; b <= nb; b++) put32(out + q + 4 * b, (uint32_t)boff[b]);
+        free(boff);
     }
     /* header (include/fz.h, struct fz_header) */
     put32(out + 0, 0x31475A46u);
@@ -485,11 +538,7 @@ int fzo_decompress(const uint8_t* st, uint64_t bytes, float* out, uint64_t n_cap
     uint16_t*       codes = (uint16_t*)calloc(n ? n : 1, 2);
     /* block offsets into Section B */
     uint64_t* boff = (uint64_t*)malloc((nb + 1) * 8);
-    uint64_t  acc  = 0;
-    for (uint64_t b = 0; b < nb; b++) {
-        boff[b] = acc;
-        for (int k = 0; k < 8; k++) acc += (uint64_t)__builtin_popcount(B[b * 8 + k]);
-    }
+    uint64_t  acc  = block_offsets(B, nb, boff);
     if (acc != nnz) {
         free(codes);
         free(boff);

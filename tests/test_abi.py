@@ -100,3 +100,32 @@ def test_header_validation_against_oracle_stream(fz, oracle, synth):
 def test_cli_usage_without_arguments(fz, lib):
     r = subprocess.run([fz.CLI_PATH], capture_output=True, text=True)
     assert r.returncode == 2 and "usage" in r.stderr
+
+
+def test_header_with_wrapping_dims_rejected(fz, oracle, synth):
+    """Dims whose product wraps 64 bits (8 * 2^30 * 2^31 = 2^64) must not pass as a small
+    field: header validation -- the check every decompression makes before it launches
+    anything -- reports a corrupt stream."""
+    st = oracle.compress(synth.smooth3d(20, 10, 8, seed=4), (20, 10, 8), 1e-3)
+    h = fz.parse_header(st)
+    h.x, h.y, h.z = 8, 1 << 30, 1 << 31
+    with pytest.raises(fz.FzError) as e:
+        fz.stream_bytes(h)
+    assert e.value.status == fz.CORRUPT_STREAM
+    h.x, h.y, h.z = 1 << 31, 1 << 31, 4  # x*y alone exceeds n
+    with pytest.raises(fz.FzError):
+        fz.stream_bytes(h)
+    v = C.c_uint64()
+    assert fz.lib().fz_max_compressed_bytes(1 << 20, fz.Dims(8, 1 << 30, 1 << 31), 1, C.byref(v)) == fz.INVALID_ARG
+
+
+def test_header_marked_failed_rejected(fz, oracle, synth):
+    """A stream whose compressing kernels reported a failure carries FZ_FLAG_FAILED in its
+    header; readers reject it."""
+    st = oracle.compress(synth.smooth2d(64, 64, seed=5), (64, 64, 1), 1e-3)
+    h = fz.parse_header(st)
+    assert fz.stream_bytes(h) == st.size
+    h.flags |= fz.FLAG_FAILED
+    with pytest.raises(fz.FzError) as e:
+        fz.stream_bytes(h)
+    assert e.value.status == fz.CORRUPT_STREAM

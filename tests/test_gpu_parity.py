@@ -119,10 +119,15 @@ FULL = [
     ("hurricane-like 500x500x100", "smooth3d", (500, 500, 100), 2, 1e-2),
     ("hurricane-like 500x500x100", "smooth3d", (500, 500, 100), 2, 1e-3),
     ("hurricane-like 500x500x100", "smooth3d", (500, 500, 100), 2, 1e-4),
+    # rows that are not a multiple of 4 elements: the whole-block paths with per-element
+    # positions and scalar halo loads, at full size
+    ("cesm-like 3601x1800", "smooth2d", (3601, 1800, 1), 0, 1e-3),
+    ("exafel-like 39201x388", "peaks2d", (39201, 388, 1), 1, 1e-3),
+    ("hurricane-like 501x500x100", "smooth3d", (501, 500, 100), 2, 1e-3),
 ]
 
 
-@pytest.mark.parametrize("name,kind,dims,seed,eb", FULL, ids=[f"{f[0].split()[0]}-{f[4]}" for f in FULL])
+@pytest.mark.parametrize("name,kind,dims,seed,eb", FULL, ids=[f"{f[0].split()[1]}-{f[4]}" for f in FULL])
 def test_full_size_workloads(fz, oracle, synth, ws, name, kind, dims, seed, eb):
     data = synth.field(kind, dims, seed)
     st, got, want = run_both(fz, oracle, ws, data, dims, eb, mode=1)
@@ -252,6 +257,27 @@ def test_nonfinite_input_relative_bound(fz, oracle, synth, ws, n):
             assert e.value.status == fz.NONFINITE_INPUT, (bad, pos)
         st, got, want = run_both(fz, oracle, ws, base, (n, 1, 1), 1e-3)
         assert_same_stream(got, want)
+
+
+def test_failure_without_readback_marks_the_stream(fz, ws):
+    """fz_compress without out_bytes does not wait: NaN in a relative-eb input then marks
+    the header FZ_FLAG_FAILED (readers reject the stream) and the workspace status reports
+    FZ_NONFINITE_INPUT; the next call's header is clean."""
+    y = torch.linspace(0, 1, 9000, device="cuda")
+    y[4000] = float("nan")
+    out = fz.compress(y, (9000, 1, 1), 1e-3, rel=True, ws=ws, readback=False)
+    torch.cuda.synchronize()
+    h = fz.parse_header(out[:64].cpu().numpy())
+    assert h.flags & fz.FLAG_FAILED
+    with pytest.raises(fz.FzError) as e:
+        fz.stream_bytes(h)
+    assert e.value.status == fz.CORRUPT_STREAM
+    assert ws.status() == fz.NONFINITE_INPUT
+    y[4000] = 0.5
+    out = fz.compress(y, (9000, 1, 1), 1e-3, rel=True, ws=ws, readback=False)
+    torch.cuda.synchronize()
+    assert not fz.parse_header(out[:64].cpu().numpy()).flags & fz.FLAG_FAILED
+    assert ws.status() == fz.SUCCESS
 
 
 def test_errors_are_statuses(fz, ws):

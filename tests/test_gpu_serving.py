@@ -27,12 +27,26 @@ def _run(fz, server, reqs):
     return done
 
 
+def _oracle_results(oracle, items):
+    """The oracle's stream and reconstruction of every field: what each served result must
+    equal, alone and in the mix."""
+    streams = [oracle.compress(d, dims, eb) for d, dims, eb in items]
+    return streams, [oracle.decompress(s) for s in streams]
+
+
 @pytest.mark.parametrize("budget_mb,slots", [(512, 4), (24, 2)])
-def test_results_identical_alone_and_in_the_mix(fz, synth, budget_mb, slots):
+def test_results_identical_alone_and_in_the_mix(fz, oracle, synth, budget_mb, slots):
+    """Served streams are byte-identical, and served reconstructions bit-identical, to the
+    oracle's, both for requests served alone and for the same requests interleaved under a
+    budget that forces queueing."""
     items = _fields(synth)
     ws = fz.Workspace(max(d.size for d, _, _ in items))
     alone = [fz.compress_host(d, dims, eb, ws=ws) for d, dims, eb in items]
     alone_rec = [fz.decompress_host(s, ws=ws) for s in alone]
+    want, want_rec = _oracle_results(oracle, items)
+    for a, ar, w, wr in zip(alone, alone_rec, want, want_rec):
+        assert np.array_equal(a, w)
+        assert np.array_equal(ar.view(np.uint32), wr.view(np.uint32))
     hin = [torch.from_numpy(d).pin_memory() for d, _, _ in items]
     caps = [fz.max_compressed_bytes(d.size, dims) for d, dims, _ in items]
     hout = [torch.empty(c, dtype=torch.uint8).pin_memory() for c in caps]
@@ -48,11 +62,11 @@ def test_results_identical_alone_and_in_the_mix(fz, synth, budget_mb, slots):
     done = _run(fz, server, reqs)
     for i, (d, _, _) in enumerate(items):
         st, nb = done[2 * i]
-        assert st == fz.SUCCESS and nb == alone[i].size
-        assert np.array_equal(hout[i][:nb].numpy(), alone[i])
+        assert st == fz.SUCCESS and nb == want[i].size
+        assert np.array_equal(hout[i][:nb].numpy(), want[i])
         st, nb = done[2 * i + 1]
         assert st == fz.SUCCESS and nb == d.size
-        assert np.array_equal(hrec[i].numpy().view(np.uint32), alone_rec[i].view(np.uint32))
+        assert np.array_equal(hrec[i].numpy().view(np.uint32), want_rec[i].view(np.uint32))
     q, r, used = server.pending()
     assert (q, r, used) == (0, 0, 0)
     server.close()
@@ -70,15 +84,19 @@ def test_request_larger_than_the_budget_is_rejected(fz, synth):
 
 
 @pytest.mark.parametrize("budget_mb,slots", [(512, 4), (12, 3)])
-def test_device_resident_requests_match_and_mix_with_host_ones(fz, synth, budget_mb, slots):
+def test_device_resident_requests_match_and_mix_with_host_ones(fz, oracle, synth, budget_mb, slots):
     """FZ_REQUEST_DEVICE: fields already in HBM compress into device streams and decompress
-    back in place; the streams equal fz_compress's and the reconstructions equal
-    fz_decompress's, alone and interleaved with host-buffer requests."""
+    back in place; the streams equal the oracle's and the reconstructions equal the
+    oracle's, alone and interleaved with host-buffer requests."""
     items = _fields(synth)
     ws = fz.Workspace(max(d.size for d, _, _ in items))
     xd = [torch.from_numpy(d).cuda() for d, _, _ in items]
     alone = [fz.compress(x, dims, eb, ws=ws) for x, (_, dims, eb) in zip(xd, items)]
     alone_rec = [fz.decompress(s, ws=ws) for s in alone]
+    want, want_rec = _oracle_results(oracle, items)
+    for a, ar, w, wr in zip(alone, alone_rec, want, want_rec):
+        assert np.array_equal(a.cpu().numpy(), w)
+        assert np.array_equal(ar.cpu().numpy().view(np.uint32), wr.view(np.uint32))
     caps = [fz.max_compressed_bytes(d.size, dims) for d, dims, _ in items]
     sd = [torch.zeros(c, dtype=torch.uint8, device="cuda") for c in caps]
     rd = [torch.zeros(d.size, dtype=torch.float32, device="cuda") for d, _, _ in items]
@@ -104,12 +122,12 @@ def test_device_resident_requests_match_and_mix_with_host_ones(fz, synth, budget
     torch.cuda.synchronize()
     for i, (d, _, _) in enumerate(items):
         st, nb = done[4 * i]
-        assert st == fz.SUCCESS and nb == alone[i].numel()
-        assert torch.equal(sd[i][:nb], alone[i])
+        assert st == fz.SUCCESS and nb == want[i].size
+        assert np.array_equal(sd[i][:nb].cpu().numpy(), want[i])
         for k, rec in ((1, rd[i].cpu()), (2, hrec[i]), (3, rd2[i].cpu())):
             st, nb = done[4 * i + k]
             assert st == fz.SUCCESS and nb == d.size
-            assert np.array_equal(rec.numpy().view(np.uint32), alone_rec[i].cpu().numpy().view(np.uint32))
+            assert np.array_equal(rec.numpy().view(np.uint32), want_rec[i].view(np.uint32))
     assert server.pending() == (0, 0, 0)
     server.close()
 

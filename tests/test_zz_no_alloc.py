@@ -48,3 +48,31 @@ def test_noalloc_rejects_fields_beyond_its_scratch(fz):
                                       fz.MODE_SIDECAR, C.c_void_p(out.data_ptr()), 1 << 40, None,
                                       fz._stream_handle(None))
     assert st == fz.INVALID_ARG
+
+
+def test_noalloc_failure_without_readback_marks_the_stream(fz, synth):
+    """With out_bytes NULL the call returns without waiting, so a failure found on the
+    device (here NaN in a relative-eb input) is recorded in the stream: its header gets
+    FZ_FLAG_FAILED and readers reject it.  The next call on the shared scratch is clean."""
+    good = synth.smooth2d(700, 300, seed=34)
+    bad = good.copy()
+    bad[4321] = np.nan
+    dims = (700, 300, 1)
+    cap = fz.max_compressed_bytes(good.size, dims, fz.MODE_SIDECAR)
+    for data, failed in ((bad, True), (good, False)):
+        x = torch.from_numpy(data).cuda()
+        out = torch.zeros(cap, dtype=torch.uint8, device="cuda")
+        st = fz.lib().fz_compress_noalloc(C.c_void_p(x.data_ptr()), x.numel(), fz._dims(dims), 1e-3, fz.EB_REL,
+                                          fz.MODE_SIDECAR, C.c_void_p(out.data_ptr()), cap, None,
+                                          fz._stream_handle(None))
+        assert st == fz.SUCCESS
+        torch.cuda.synchronize()
+        h = fz.parse_header(out[:64].cpu().numpy())
+        assert bool(h.flags & fz.FLAG_FAILED) == failed
+        if failed:
+            with pytest.raises(fz.FzError) as e:
+                fz.stream_bytes(h)
+            assert e.value.status == fz.CORRUPT_STREAM
+        else:
+            want = fz.compress(x, dims, 1e-3).cpu().numpy()
+            assert np.array_equal(out[: want.size].cpu().numpy(), want)
