@@ -117,6 +117,8 @@ SIGNATURES = {
     "fz_batch_create_ex": (_I, [_P, _P, _U32, _I, _I, _I, _U32, C.POINTER(_P)]),
     "fz_batch_create_pair": (_I, [_P, _P, _P, _U32, _I, _I, _U32, C.POINTER(_P)]),
     "fz_batch_autotune": (_I, [_P, _P, _U32, _I, _I, _I, _U32, _P, C.POINTER(_U32), C.POINTER(C.c_double)]),
+    "fz_batch_create_sched": (_I, [_P, _P, _P, _U32, _I, _I, C.c_void_p, C.POINTER(_P)]),
+    "fz_batch_autotune_sched": (_I, [_P, _P, _P, _U32, _I, _I, _U32, _P, C.c_void_p, C.POINTER(C.c_double)]),
     "fz_server_create": (_I, [_U64, _U32, _U64, C.POINTER(_P)]),
     "fz_server_submit": (_I, [_P, C.POINTER(Request)]),
     "fz_server_poll": (_I, [_P, C.POINTER(Completion), _U32, C.POINTER(C.c_uint32)]),
@@ -227,9 +229,10 @@ class Workspace:
         """Status of a look-back that waits on a tile nothing publishes (FZ_TIMEOUT)."""
         return lib().fz_selftest_wait_timeout(self.handle, _stream_handle(stream))
 
-    # timing kinds of fz_workspace_kernel_time, by the kernels they time: k_encode<ND> and
-    # k_decompress{1,2,3}d are templated / specialised per dimensionality
-    KERNELS = ("k_range", "k_encode", "k_offsets", "k_decompress", "k_recon", "k_compact")
+    # timing kinds of fz_workspace_kernel_time, by the kernels they time:
+    # k_encode_fields<ND> and k_decompress{1,2,3}d are templated / specialised per
+    # dimensionality
+    KERNELS = ("k_range_fields", "k_encode_fields", "k_offsets", "k_decompress", "k_recon", "k_compact_fields")
 
     def enable_timing(self, capacity):
         _check("fz_workspace_enable_timing", lib().fz_workspace_enable_timing(self.handle, int(capacity)))
@@ -417,6 +420,22 @@ def batch_autotune(ws, fields, direction, rel=True, mode=MODE_SIDECAR, reps=3, s
     return best.value, {b: ms[i] for i, b in enumerate((1, 2, 4, 8, 16)) if ms[i] > 0}
 
 
+class Schedule(C.Structure):
+    """fz_batch_schedule: parallel branches, and whether the compression runs as list
+    launches over all fields."""
+    _fields_ = [("branches", C.c_uint32), ("list", C.c_uint32)]
+
+
+def batch_autotune_schedule(ws, comp=None, dec=None, rel=True, mode=MODE_SIDECAR, reps=3, stream=None):
+    """fz_batch_autotune_sched: (best Schedule, {(branches, list): mean replay ms})."""
+    best, ms = Schedule(), (C.c_double * 10)()
+    n = len(comp) if comp is not None else len(dec)
+    _check("fz_batch_autotune_sched", lib().fz_batch_autotune_sched(ws.handle, comp, dec, n, EB_REL if rel else EB_ABS,
+                                                                    mode, int(reps), _stream_handle(stream),
+                                                                    C.byref(best), ms))
+    return best, {((1, 2, 4, 8, 16)[i % 5], i // 5): ms[i] for i in range(10) if ms[i] > 0}
+
+
 class Batch:
     """A batch recorded once into a CUDA graph (fz_batch_create / fz_batch_create_ex with
     `branches` parallel branches, 0 = default) and replayed."""
@@ -439,6 +458,20 @@ class Batch:
         _check("fz_batch_create_pair", lib().fz_batch_create_pair(ws.handle, comp, dec, len(comp),
                                                                   EB_REL if rel else EB_ABS, mode, int(branches),
                                                                   C.byref(h)))
+        self.handle = h
+        return self
+
+    @classmethod
+    def scheduled(cls, ws, comp=None, dec=None, schedule=None, rel=True, mode=MODE_SIDECAR):
+        """fz_batch_create_sched: compression of comp and/or decompression of dec under a
+        Schedule (default: 8 branches, per-field compression)."""
+        self = cls.__new__(cls)
+        self.ws, self.fields = ws, (comp, dec)
+        sch = schedule if schedule is not None else Schedule(0, 0)
+        n = len(comp) if comp is not None else len(dec)
+        h = C.c_void_p()
+        _check("fz_batch_create_sched", lib().fz_batch_create_sched(ws.handle, comp, dec, n, EB_REL if rel else EB_ABS,
+                                                                    mode, C.byref(sch), C.byref(h)))
         self.handle = h
         return self
 

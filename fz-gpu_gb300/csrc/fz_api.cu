@@ -219,7 +219,7 @@ fz_status fz_workspace_bytes(uint64_t max_n, uint64_t* bytes)
     const uint64_t tiles = max_n / kBlockCodes + 2;
     uint64_t       b     = 0;
     b += pad16(8 * tiles);          // state
-    b += 64;                        // tickets, status, total
+    b += 128;                       // tickets, status, total, field control words
     b += 16;                        // range accumulators
     b += pad16(2 * max_n + 16);     // per-block slots (k_encode)
     b += pad16(4 * tiles + 4);      // block offsets
@@ -255,7 +255,8 @@ fz_status fz_workspace_create(uint64_t max_n, fz_workspace** out)
     ws->epoch   = ws->tickets + 6;
     ws->ovfw    = ws->tickets + 7;
     ws->done    = ws->tickets + 8;
-    p += 64;
+    ws->fctl    = reinterpret_cast<FieldCtl*>(ws->tickets + 16);
+    p += 128;
     ws->mm       = reinterpret_cast<uint32_t*>(p), p += 16;
     ws->codes    = reinterpret_cast<uint16_t*>(p), p += pad16(2 * max_n + 16);
     ws->boff     = reinterpret_cast<uint32_t*>(p), p += pad16(4ull * ws->max_tiles + 4);
@@ -264,6 +265,7 @@ fz_status fz_workspace_create(uint64_t max_n, fz_workspace** out)
     if (e == cudaSuccess) {
         const uint32_t init[2] = {0xFFFFFFFFu, 0u};  // empty min/max
         e                      = cudaMemcpy(ws->mm, init, sizeof(init), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(ws->fctl->mm, init, sizeof(init), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = cudaMallocHost((void**)&ws->h_pinned, 128);
     if (e != cudaSuccess) {
@@ -355,24 +357,20 @@ fz_status fz_compress(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims d
 
 }  // extern "C"
 
-// fz_compress with an optional device mirror of the header and status word (128 bytes,
-// written by the last kernel; the request loop reads both with one copy).
-fz_status fz::compress_impl(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims dims, double eb,
-                            fz_eb_mode eb_mode, fz_mode mode, void* d_out, uint64_t out_capacity,
-                            uint64_t* out_bytes, fz_stream_t stream, uint32_t* mirror)
+// Checks the arguments of one field's compression and fills its layout and kernel
+// arguments (without the scan state and mirror, which depend on the caller).
+static fz_status compress_args(const float* d_in, uint64_t n, fz_dims dims, double eb, fz_eb_mode eb_mode,
+                               fz_mode mode, void* d_out, uint64_t out_capacity, uint32_t* status, Layout& L,
+                               CompressArgs& a)
 {
-    if (!ws || !d_in || !d_out || !aligned16(d_in) || !aligned16(d_out)) return FZ_INVALID_ARG;
-    if (check_dims(n, dims) != FZ_SUCCESS || n > ws->max_n) return FZ_INVALID_ARG;
+    if (!d_in || !d_out || !aligned16(d_in) || !aligned16(d_out)) return FZ_INVALID_ARG;
+    if (check_dims(n, dims) != FZ_SUCCESS) return FZ_INVALID_ARG;
     if (!(eb > 0) || !std::isfinite(eb)) return FZ_INVALID_ARG;
     if ((eb_mode != FZ_EB_ABS && eb_mode != FZ_EB_REL) || (mode != FZ_MODE_COMPAT && mode != FZ_MODE_SIDECAR))
         return FZ_INVALID_ARG;
-    fz_status st = check_device(ws);
-    if (st != FZ_SUCCESS) return st;
-    const Layout L = make_layout(n, dims.x, dims.y, dims.z, mode);
+    L = make_layout(n, dims.x, dims.y, dims.z, mode);
     if (out_capacity < max_stream(L)) return FZ_OUT_OF_SPACE;
-    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-
-    CompressArgs a{};
+    a    = CompressArgs{};
     a.in = d_in, a.out = static_cast<uint8_t*>(d_out);
     a.n = L.n, a.nl = L.nl, a.x = L.x, a.y = L.y, a.z = L.z, a.xy = L.xy;
     a.dx = make_fastdiv(L.x), a.dxy = make_fastdiv(L.xy);
@@ -380,32 +378,61 @@ fz_status fz::compress_impl(fz_workspace* ws, const float* d_in, uint64_t n, fz_
     a.nb = L.nb, a.ntiles = L.nb + (L.tail ? 1 : 0), a.nwords = L.nwords;
     a.mode = mode, a.ndim = L.ndim, a.sidecar_bytes = L.sidecar_bytes;
     a.off_a = L.off_a, a.off_c = L.off_c, a.off_b = L.off_b, a.off_sign = L.off_sign, a.off_boff = L.off_boff;
-    a.state = ws->state, a.ticket = ws->tickets + 0, a.status = ws->status, a.epoch = ws->epoch;
-    a.boff  = mode == FZ_MODE_SIDECAR ? reinterpret_cast<uint32_t*>(a.out + L.off_boff) : nullptr;
-    a.mirror = mirror;
-    cudaError_t e = cudaSuccess;
+    a.status = status;
+    a.boff   = mode == FZ_MODE_SIDECAR ? reinterpret_cast<uint32_t*>(a.out + L.off_boff) : nullptr;
+    a.mm     = nullptr;
     if (eb_mode == FZ_EB_REL) {
-        KernelTimer t(ws, s, 0);
-        e        = launch_range(d_in, L.n, ws->mm, ws->status, ws->ovfw, s);
-        a.mm     = ws->mm;
         a.eb_rel = eb;
     } else {
-        a.mm            = nullptr;
         a.ebh.eb_abs    = eb;
         const double e2 = eb * 2;  // lorenzo_var.cuh:562-563
         a.ebh.ebx2_r    = (float)(1 / e2);
         a.ebh.ebx2      = (float)e2;
         a.ebh.range = a.ebh.vmin = a.ebh.vmax = 0.0f;
     }
+    return FZ_SUCCESS;
+}
+
+// fz_compress with an optional device mirror of the header and status word (128 bytes,
+// written by the last kernel; the request loop reads both with one copy).
+fz_status fz::compress_impl(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims dims, double eb,
+                            fz_eb_mode eb_mode, fz_mode mode, void* d_out, uint64_t out_capacity,
+                            uint64_t* out_bytes, fz_stream_t stream, uint32_t* mirror)
+{
+    if (!ws) return FZ_INVALID_ARG;
+    if (n > ws->max_n) return FZ_INVALID_ARG;
+    fz_status st = check_device(ws);
+    if (st != FZ_SUCCESS) return st;
+    Layout       L;
+    CompressArgs a;
+    st = compress_args(d_in, n, dims, eb, eb_mode, mode, d_out, out_capacity, ws->status, L, a);
+    if (st != FZ_SUCCESS) return st;
+    a.state = ws->state, a.ticket = ws->tickets + 0, a.epoch = ws->epoch;
+    a.mirror = mirror;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    // the field as a list of one: range launch (relative eb), encode launch (per-block
+    // slots in the workspace scratch, one 4 KiB slot per shuffle block; chunk counts in the
+    // block-offset array), compaction launch
+    FieldJob J{};
+    J.a      = a;
+    J.ctl    = ws->fctl;
+    J.slots  = reinterpret_cast<uint4*>(ws->codes);
+    J.counts = ws->boff;
+    J.supers = ws->supers;
+    J.rel    = eb_mode == FZ_EB_REL;
+    field_items(L.n, L.nb, a.ntiles, J.rel != 0, J.nr, J.ne, J.nc);
+    cudaError_t e = cudaSuccess;
+    if (J.nr) {
+        KernelTimer t(ws, s, 0);
+        e = launch_fields(FieldPhase::Range, (int)L.ndim, nullptr, nullptr, 0, J.nr, J, s);
+    }
     if (e == cudaSuccess) {
-        // two launches: per-block slots in the workspace scratch (2 bytes per element, one 4 KiB
-        // slot per shuffle block) and per-block counts in the block-offset array
         KernelTimer t(ws, s, 1);
-        e = launch_encode(a, reinterpret_cast<uint4*>(ws->codes), ws->boff, ws->supers, ws->ovfw, s);
+        e = launch_fields(FieldPhase::Encode, (int)L.ndim, nullptr, nullptr, 0, J.ne, J, s);
     }
     if (e == cudaSuccess) {
         KernelTimer t(ws, s, 5);
-        e = launch_compact(a, reinterpret_cast<const uint4*>(ws->codes), ws->boff, ws->supers, ws->ovfw, ws->done, s);
+        e = launch_fields(FieldPhase::Compact, (int)L.ndim, nullptr, nullptr, 0, J.nc, J, s);
     }
     if (e != cudaSuccess) return map_err(e);
     if (out_bytes) {
@@ -639,10 +666,100 @@ fz_status fz_decompress_batch(fz_workspace* ws, const fz_field* fields, uint32_t
 
 }  // extern "C"
 
+namespace {
+
+// Device work list of a batch compression, in one allocation: every field's job and
+// control words, its slots (4 KiB per shuffle block), block counts and 512-block group
+// sums, and the segment tables of the range launch, of the encode launch of each
+// dimensionality and of the compaction launch.
+struct ListPlan {
+    void*    d_mem = nullptr;
+    Segment* seg[5]   = {};  // [0] range, [1..3] encode 1D..3D, [4] compaction
+    uint32_t nseg[5]  = {};
+    uint32_t total[5] = {};
+    FieldJob* jobs    = nullptr;
+};
+
+fz_status plan_list_compress(fz_workspace* ws, const fz_field* f, uint32_t count, fz_eb_mode eb_mode, fz_mode mode,
+                             ListPlan& P)
+{
+    std::vector<FieldJob> jobs(count);
+    std::vector<Layout>   lay(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const fz_status st = compress_args(static_cast<const float*>(f[i].src), f[i].n, f[i].dims, f[i].eb, eb_mode,
+                                           mode, f[i].dst, f[i].dst_capacity, ws->status, lay[i], jobs[i].a);
+        if (st != FZ_SUCCESS) return st;
+        jobs[i].rel = eb_mode == FZ_EB_REL;
+        field_items(lay[i].n, lay[i].nb, jobs[i].a.ntiles, jobs[i].rel != 0, jobs[i].nr, jobs[i].ne, jobs[i].nc);
+    }
+    // sizes: jobs | control words | segments | per field: slots, counts, group sums
+    const uint64_t b_jobs = (sizeof(FieldJob) * (uint64_t)count + 255) & ~255ull;
+    const uint64_t b_ctl  = (sizeof(FieldCtl) * (uint64_t)count + 255) & ~255ull;
+    const uint64_t b_seg  = (sizeof(Segment) * 5ull * count + 255) & ~255ull;
+    uint64_t       b_scr  = 0;
+    std::vector<uint64_t> off(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        off[i] = b_scr;
+        b_scr += 4096ull * lay[i].nb + pad16(4ull * (lay[i].nb + 2)) + pad16(4ull * (lay[i].nb / kSuperBlocks + 2));
+        b_scr = (b_scr + 255) & ~255ull;
+    }
+    uint8_t*    base = nullptr;
+    cudaError_t e    = cudaMalloc(reinterpret_cast<void**>(&base), b_jobs + b_ctl + b_seg + std::max<uint64_t>(b_scr, 16));
+    if (e != cudaSuccess) return map_err(e, FZ_FAIL_GPU_MALLOC);
+    P.d_mem        = base;
+    P.jobs         = reinterpret_cast<FieldJob*>(base);
+    FieldCtl* ctl  = reinterpret_cast<FieldCtl*>(base + b_jobs);
+    Segment*  segd = reinterpret_cast<Segment*>(base + b_jobs + b_ctl);
+    uint8_t*  scr  = base + b_jobs + b_ctl + b_seg;
+    std::vector<FieldCtl> hctl(count);
+    std::vector<Segment>  hseg;
+    for (uint32_t i = 0; i < count; ++i) {
+        hctl[i].mm[0] = 0xFFFFFFFFu;  // empty range
+        FieldJob& J   = jobs[i];
+        J.ctl         = ctl + i;
+        J.slots       = reinterpret_cast<uint4*>(scr + off[i]);
+        J.counts      = reinterpret_cast<uint32_t*>(scr + off[i] + 4096ull * lay[i].nb);
+        J.supers      = reinterpret_cast<uint32_t*>(scr + off[i] + 4096ull * lay[i].nb + pad16(4ull * (lay[i].nb + 2)));
+    }
+    for (int k = 0; k < 5; ++k) {
+        P.seg[k] = segd + hseg.size();
+        for (uint32_t i = 0; i < count; ++i) {
+            const uint32_t items = k == 0 ? jobs[i].nr : k == 4 ? jobs[i].nc : ((int)lay[i].ndim == k ? jobs[i].ne : 0u);
+            if (!items) continue;
+            hseg.push_back(Segment{P.total[k], i, items, 0u});
+            P.total[k] += items;
+            ++P.nseg[k];
+        }
+    }
+    e = cudaMemset(base, 0, b_jobs + b_ctl + b_seg + std::max<uint64_t>(b_scr, 16));  // group sums start at 0
+    if (e == cudaSuccess) e = cudaMemcpy(P.jobs, jobs.data(), sizeof(FieldJob) * count, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(ctl, hctl.data(), sizeof(FieldCtl) * count, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !hseg.empty())
+        e = cudaMemcpy(segd, hseg.data(), sizeof(Segment) * hseg.size(), cudaMemcpyHostToDevice);
+    return map_err(e);
+}
+
+// The batch's compression: one range launch over every field (relative eb), one encode
+// launch per dimensionality present, one compaction launch over every field.
+cudaError_t launch_list_compress(const ListPlan& P, cudaStream_t s)
+{
+    const FieldJob none{};
+    cudaError_t    e = cudaSuccess;
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k) {
+        if (!P.total[k]) continue;
+        const FieldPhase ph = k == 0 ? FieldPhase::Range : k == 4 ? FieldPhase::Compact : FieldPhase::Encode;
+        e = launch_fields(ph, k >= 1 && k <= 3 ? k : 2, P.jobs, P.seg[k], P.nseg[k], P.total[k], none, s);
+    }
+    return e;
+}
+
+}  // namespace
+
 struct fz_batch {
     cudaGraph_t                graph = nullptr;
     cudaGraphExec_t            exec  = nullptr;
-    std::vector<fz_workspace*> own_ws;  // the extra branches' workspaces
+    std::vector<fz_workspace*> own_ws;  // the extra branches' workspaces (decompression)
+    void*                      d_list = nullptr;  // work list of the batch's compression
 };
 
 extern "C" {
@@ -661,8 +778,11 @@ fz_status fz_batch_create(fz_workspace* ws, const fz_field* fields, uint32_t cou
 // Captures count fields into one graph: comp[i] (compression, if comp) followed by
 // dec[i] (decompression, if dec) on branch i % branches, each branch with its own
 // workspace; the fork and the join make the graph one unit on the launching stream.
+// list: the compression as list launches over every field (then decompressions, if any,
+// on the branches once all streams are written); otherwise each field's compression and
+// decompression on its branch.
 static fz_status capture_batch(fz_workspace* ws, const fz_field* comp, const fz_field* dec, uint32_t count,
-                               fz_eb_mode eb_mode, fz_mode mode, uint32_t nbranch, fz_batch* b)
+                               fz_eb_mode eb_mode, fz_mode mode, uint32_t nbranch, bool list, fz_batch* b)
 {
     const uint32_t branches = std::max(1u, std::min(nbranch ? nbranch : kBatchBranches, count));
     uint64_t       max_n    = 1;
@@ -670,8 +790,15 @@ static fz_status capture_batch(fz_workspace* ws, const fz_field* comp, const fz_
         if (comp) max_n = std::max<uint64_t>(max_n, comp[i].n);
         if (dec) max_n = std::max<uint64_t>(max_n, dec[i].header.n);
     }
+    fz_status st = check_device(ws);
+    if (st != FZ_SUCCESS) return st;
+    ListPlan plan;
+    if (list && comp && count) {
+        st        = plan_list_compress(ws, comp, count, eb_mode, mode, plan);
+        b->d_list = plan.d_mem;
+        if (st != FZ_SUCCESS) return st;
+    }
     std::vector<fz_workspace*> wss{ws};
-    fz_status                  st = FZ_SUCCESS;
     for (uint32_t i = 1; i < branches && st == FZ_SUCCESS; ++i) {
         fz_workspace* w = nullptr;
         st              = fz_workspace_create(std::max(max_n, (uint64_t)1), &w);
@@ -691,13 +818,18 @@ static fz_status capture_batch(fz_workspace* ws, const fz_field* comp, const fz_
         cudaError_t e = cudaStreamBeginCapture(cs[0], cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) st = map_err(e);
         else {
-            // fork
+            // list schedule: the whole compression in a handful of list launches
+            if (plan.d_mem) {
+                e = launch_list_compress(plan, cs[0]);
+                if (e != cudaSuccess) st = map_err(e);
+            }
+            // fork: per-field work on parallel branches
             cudaEventRecord(ev[0], cs[0]);
             for (uint32_t i = 1; i < branches; ++i) cudaStreamWaitEvent(cs[i], ev[0], 0);
             for (uint32_t i = 0; i < count && st == FZ_SUCCESS; ++i) {
                 const uint32_t k = i % branches;
                 fz_stream_t    h = reinterpret_cast<fz_stream_t>(cs[k]);
-                if (comp) st = fz_compress_batch(wss[k], comp + i, 1, eb_mode, mode, h);
+                if (comp && !plan.d_mem) st = fz_compress_batch(wss[k], comp + i, 1, eb_mode, mode, h);
                 if (dec && st == FZ_SUCCESS) st = fz_decompress_batch(wss[k], dec + i, 1, h);
             }
             // join
@@ -732,7 +864,7 @@ fz_status fz_batch_create_ex(fz_workspace* ws, const fz_field* fields, uint32_t 
     fz_batch* b = new (std::nothrow) fz_batch();
     if (!b) return FZ_FAIL_GPU_MALLOC;
     const fz_status st = capture_batch(ws, dir == FZ_COMPRESS ? fields : nullptr, dir == FZ_DECOMPRESS ? fields : nullptr,
-                                       count, eb_mode, mode, nbranch, b);
+                                       count, eb_mode, mode, nbranch, false, b);
     if (st != FZ_SUCCESS) {
         fz_batch_destroy(b);
         return st;
@@ -749,13 +881,73 @@ fz_status fz_batch_create_pair(fz_workspace* ws, const fz_field* comp, const fz_
     *out = nullptr;
     fz_batch* b = new (std::nothrow) fz_batch();
     if (!b) return FZ_FAIL_GPU_MALLOC;
-    const fz_status st = capture_batch(ws, comp, dec, count, eb_mode, mode, nbranch, b);
+    const fz_status st = capture_batch(ws, comp, dec, count, eb_mode, mode, nbranch, false, b);
     if (st != FZ_SUCCESS) {
         fz_batch_destroy(b);
         return st;
     }
     *out = b;
     return FZ_SUCCESS;
+}
+
+fz_status fz_batch_create_sched(fz_workspace* ws, const fz_field* comp, const fz_field* dec, uint32_t count,
+                                fz_eb_mode eb_mode, fz_mode mode, const fz_batch_schedule* sched, fz_batch** out)
+{
+    if (!ws || !out || !sched || (!comp && !dec)) return FZ_INVALID_ARG;
+    if (sched->branches > FZ_BATCH_MAX_BRANCHES || sched->list > 1) return FZ_INVALID_ARG;
+    *out = nullptr;
+    fz_batch* b = new (std::nothrow) fz_batch();
+    if (!b) return FZ_FAIL_GPU_MALLOC;
+    const fz_status st = capture_batch(ws, comp, dec, count, eb_mode, mode, sched->branches, sched->list != 0, b);
+    if (st != FZ_SUCCESS) {
+        fz_batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return FZ_SUCCESS;
+}
+
+fz_status fz_batch_autotune_sched(fz_workspace* ws, const fz_field* comp, const fz_field* dec, uint32_t count,
+                                  fz_eb_mode eb_mode, fz_mode mode, uint32_t reps, fz_stream_t stream,
+                                  fz_batch_schedule* best, double* ms)
+{
+    if (!ws || !best || !count || (!comp && !dec) || !reps) return FZ_INVALID_ARG;
+    static constexpr uint32_t kCand[5] = {1, 2, 4, 8, 16};
+    cudaStream_t s  = reinterpret_cast<cudaStream_t>(stream);
+    cudaEvent_t  e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return FZ_FAIL_GPU_ILLEGAL_ACCESS;
+    }
+    fz_status st     = FZ_SUCCESS;
+    float     best_t = 0;
+    *best            = fz_batch_schedule{0, 0};
+    for (int c = 0; c < 10 && st == FZ_SUCCESS; ++c) {
+        if (ms) ms[c] = 0;
+        const fz_batch_schedule cand{kCand[c % 5], (uint32_t)(c / 5)};
+        if (cand.branches > count && c % 5 > 0) continue;  // the same graph as a smaller candidate
+        if (cand.list && !comp) continue;                   // nothing to list without compression
+        fz_batch* b = nullptr;
+        st          = fz_batch_create_sched(ws, comp, dec, count, eb_mode, mode, &cand, &b);
+        if (st != FZ_SUCCESS) break;
+        st = fz_batch_launch(b, stream);  // warm-up
+        cudaError_t e = st == FZ_SUCCESS ? cudaEventRecord(e0, s) : cudaSuccess;
+        for (uint32_t r = 0; r < reps && st == FZ_SUCCESS && e == cudaSuccess; ++r) st = fz_batch_launch(b, stream);
+        if (st == FZ_SUCCESS && e == cudaSuccess) e = cudaEventRecord(e1, s);
+        if (st == FZ_SUCCESS && e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float t = 0;
+        if (st == FZ_SUCCESS && e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+        if (st == FZ_SUCCESS && e != cudaSuccess) st = map_err(e);
+        if (st == FZ_SUCCESS) {
+            t /= (float)reps;
+            if (ms) ms[c] = t;
+            if (best->branches == 0 || t < best_t) *best = cand, best_t = t;
+        }
+        fz_batch_destroy(b);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return st;
 }
 
 fz_status fz_batch_launch(fz_batch* b, fz_stream_t stream)
@@ -770,6 +962,7 @@ fz_status fz_batch_destroy(fz_batch* b)
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     for (fz_workspace* w : b->own_ws) fz_workspace_destroy(w);
+    if (b->d_list) cudaFree(b->d_list);
     delete b;
     return FZ_SUCCESS;
 }

@@ -976,67 +976,23 @@ __global__ void __launch_bounds__(kCompressWarps * 32, 3) k_compress(const Compr
     }
 }
 
-// ====================================================== two-kernel compress ==
-// The workspace path splits compression in two launches so that no warp ever waits for
-// a look-back:
-//   k_encode   one CTA per scan tile (8 shuffle blocks, one per warp), independent of
-//              all others: phases A-C of compute_block (codes, transpose, chunk flags,
-//              bitmap words, sidecar), then the block's non-zero chunks, compacted, into
-//              its own 4 KiB slot of the workspace scratch and its chunk count into
-//              counts[t].  Overflow bits are OR-ed into one word.
-//              Each block's count is also added into the sum of its super-tile (512
-//              blocks).
-//   k_compact  every block's exclusive chunk offset -- the super-tile sums before its
-//              super-tile plus the counts inside it before the block: all known, so no
-//              CTA waits for another --, the offset table, the move of every block's
-//              chunks from its slot to Section B, and (last CTA to finish) the header.
-// The stream bytes equal the fused kernel's.
-constexpr uint32_t kCompactBlocks = 32;   // shuffle blocks per k_compact CTA
-constexpr uint32_t kSuperBlocks   = 512;  // shuffle blocks per super-tile sum
+// ================================================ list compression ==
+// Compression of a list of fields in three launches, each a persistent grid striding over
+// a device work list (FieldJob / Segment, fz_internal.h):
+//   k_range_fields     range items: max/min of a 16384-element chunk (relative eb)
+//   k_encode_fields    encode items: 8 shuffle blocks, one per warp -- codes, bitshuffle,
+//                      chunk flags, bitmap words, sidecar, the block's non-zero chunks
+//                      compacted into its own 4 KiB slot, its count into counts[] and the
+//                      sum of its 512-block group; no CTA waits for another
+//   k_compact_fields   compaction items: 32 blocks -- every block's chunk offset (all
+//                      counts are known: the group sums before it plus the counts in its
+//                      group), the offset table, the chunks moved from the slots to
+//                      Section B; the field's last item writes the header
+// A single field is a list of one whose job is a kernel parameter.  The stream bytes equal
+// the single-pass look-back kernel's.
+constexpr uint32_t kCompactBlocks = 32;   // shuffle blocks per compaction item
 
-template <int ND>
-__global__ void __launch_bounds__(kCompressWarps * 32, ND == 3 ? 4 : 5) k_encode(const CompressArgs a, uint4* slots,
-                                                                    uint32_t* counts, uint32_t* supers,
-                                                                    uint32_t* ovfw)
-{
-    __shared__ __align__(16) uint32_t smem[kCompressWarps][kBlockWords];
-    __shared__ float s_r;
-    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-    if (threadIdx.x == 0)
-        s_r = a.mm ? eb_from_range(ord2f(__ldcg(a.mm)), ord2f(__ldcg(a.mm + 1)), a.eb_rel).ebx2_r : a.ebh.ebx2_r;
-    __syncthreads();
-    Geo g;
-    g.nl = a.nl, g.x = a.x, g.y = a.y, g.xy = a.xy, g.lim = a.n;
-    g.dx = a.dx, g.dxy = a.dxy, g.al_x = a.al_x, g.al_xy = a.al_xy, g.al_xyx = a.al_xyx;
-    uint32_t*      signw = (ND == 1 && a.mode == 1) ? reinterpret_cast<uint32_t*>(a.out + a.off_sign) : nullptr;
-    const uint32_t t     = blockIdx.x * kCompressWarps + wid;
-    uint32_t       bm[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cnt = 0, ovf = 0;
-    compute_block<ND>(a, g, t, s_r, lane, smem[wid], signw, bm, cnt, ovf);  // warp-uniform t
-    if (t < a.nb) {
-        uint4*         S   = slots + (size_t)t * kChunks;
-        const uint32_t lt  = lanemask_lt();
-        uint32_t       pre = 0;
-#pragma unroll
-        for (uint32_t i = 0; i < 8; ++i) {
-            if ((bm[i] >> lane) & 1u)
-                S[pre + __popc(bm[i] & lt)] = *reinterpret_cast<const uint4*>(smem[wid] + (lane + 32 * i) * 4);
-            pre += __popc(bm[i]);
-        }
-        if (lane == 0) {
-            counts[t] = cnt;
-            if (cnt) atomicAdd(supers + t / kSuperBlocks, cnt);
-        }
-    }
-    if (ovf && lane == 0) atomicOr(ovfw, 1u);
-}
-
-// One CTA per kCompactBlocks blocks; no CTA waits for another.  The CTA's first offset is
-// the sum of the super-tile sums before its super-tile plus the counts of the blocks of
-// its super-tile before it (block reductions); warp 0 scans its 32 counts.  All threads
-// then move the CTA's chunks: output chunk q comes from block j = the last with
-// pre[j] <= q, four independent 16-byte loads in flight per thread.  The last CTA to
-// finish writes the header and the offset table's total, and leaves the super-tile
-// sums, the overflow word, the done counter and the range accumulators reset.
+// Sum of v over the CTA (256 threads), in every thread.
 __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red)
 {
     v = __reduce_add_sync(kFull, v);
@@ -1046,33 +1002,144 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red)
     return __reduce_add_sync(kFull, (threadIdx.x & 31u) < kCompressWarps ? red[threadIdx.x & 31u] : 0u);
 }
 
-__global__ void __launch_bounds__(256) k_compact(const CompressArgs a, const uint4* slots, const uint32_t* counts,
-                                                 uint32_t* supers, uint32_t* ovfw, uint32_t* done)
+// ---------------------------------------------------------------- items --
+constexpr uint32_t kCtlOverflow    = 1u << 8;                    // FieldCtl::flags: some code overflowed
+constexpr uint32_t kRangeVec       = 8;                          // 16-byte loads in flight per thread
+constexpr uint32_t kRangeRounds    = 2;                          // rounds per range item
+constexpr uint32_t kRangeItemElems = 256 * kRangeVec * 4 * kRangeRounds;  // 16384
+
+void field_items(uint32_t n, uint32_t nb, uint32_t ntiles, bool rel, uint32_t& nr, uint32_t& ne, uint32_t& nc)
 {
-    static_assert(kCompactBlocks == 32 && kSuperBlocks % kCompactBlocks == 0, "one warp scans the CTA's counts");
-    __shared__ uint32_t s_red[kCompressWarps], s_tot, s_pre[kCompactBlocks], s_last;
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, wid = tid >> 5;
-    const uint32_t b0 = blockIdx.x * kCompactBlocks, sup = b0 / kSuperBlocks;
-    // warp 0's own counts are loaded together with everyone's prefix terms
-    const uint32_t c = (wid == 0 && b0 + lane < a.nb) ? __ldcg(counts + b0 + lane) : 0u;
-    uint32_t       acc = 0;
-    for (uint32_t i = tid; i < sup; i += blockDim.x) acc += __ldcg(supers + i);
-    for (uint32_t b = sup * kSuperBlocks + tid; b < b0; b += blockDim.x) acc += __ldcg(counts + b);
-    const uint32_t excl = block_sum(acc, s_red);
+    nr = rel ? (uint32_t)std::max<uint64_t>(1, cdiv(n, kRangeItemElems)) : 0u;
+    ne = (uint32_t)cdiv(ntiles, kCompressWarps);
+    nc = (uint32_t)std::max<uint64_t>(1, cdiv(nb, kCompactBlocks));
+}
+
+// Item k of a list launch: field f owns items [segs[f].start, segs[f].start + segs[f].count)
+// of the launch (segments sorted by start).  Binary search; the result is CTA-uniform.
+__device__ __forceinline__ void locate(const Segment* __restrict__ segs, uint32_t nseg, uint32_t k, uint32_t& f,
+                                       uint32_t& i)
+{
+    uint32_t lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(&segs[mid].start) <= k) lo = mid;
+        else hi = mid - 1;
+    }
+    f = __ldg(&segs[lo].field);
+    i = k - __ldg(&segs[lo].start);
+}
+
+// Range item i: max/min of elements [i*16384, (i+1)*16384) (the last item also takes the
+// n mod 4 elements past the 16-byte loads) folded into the field's accumulators.
+__device__ __forceinline__ void range_item(const FieldJob& J, uint32_t i, uint32_t (*sred)[kCompressWarps])
+{
+    const float*   in = J.a.in;
+    const uint32_t n = J.a.n, n4 = n / 4, tid = threadIdx.x;
+    float          mn = INFINITY, mx = -INFINITY;
+#pragma unroll 1
+    for (uint32_t rd = 0; rd < kRangeRounds; ++rd) {
+        const uint32_t b0 = i * (kRangeItemElems / 4) + rd * (256 * kRangeVec) + tid;
+        float4         v[kRangeVec];
+#pragma unroll
+        for (uint32_t k = 0; k < kRangeVec; ++k)
+            if (b0 + k * 256 < n4) v[k] = ldg4(in + 4 * (size_t)(b0 + k * 256));
+#pragma unroll
+        for (uint32_t k = 0; k < kRangeVec; ++k) {
+            if (b0 + k * 256 >= n4) continue;
+            mn = fmin_nan(fmin_nan(mn, v[k].x), fmin_nan(v[k].y, fmin_nan(v[k].z, v[k].w)));
+            mx = fmax_nan(fmax_nan(mx, v[k].x), fmax_nan(v[k].y, fmax_nan(v[k].z, v[k].w)));
+        }
+    }
+    // NaN leaves both NaN; -Inf shows in the min, +Inf in the max
+    uint32_t nonfinite = (mn != mn) | (mn == -INFINITY) | (mx == INFINITY);
+    if ((i + 1) * kRangeItemElems >= n && tid < n - 4 * n4) {
+        const float v = in[4 * n4 + tid];
+        mn = fminf(mn, v), mx = fmaxf(mx, v);
+        nonfinite |= !isfinite(v);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(kFull, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+    }
+    nonfinite = __reduce_or_sync(kFull, nonfinite);
+    const uint32_t lane = tid & 31u, wid = tid >> 5;
+    if (lane == 0) sred[0][wid] = f2ord(mn), sred[1][wid] = f2ord(mx), sred[2][wid] = nonfinite;
+    __syncthreads();
+    if (tid < 32) {
+        const uint32_t a = __reduce_min_sync(kFull, lane < kCompressWarps ? sred[0][lane] : 0xFFFFFFFFu);
+        const uint32_t c = __reduce_max_sync(kFull, lane < kCompressWarps ? sred[1][lane] : 0u);
+        const uint32_t f = __reduce_or_sync(kFull, lane < kCompressWarps ? sred[2][lane] : 0u);
+        if (lane == 0) {
+            atomicMin(J.ctl->mm, a);
+            atomicMax(J.ctl->mm + 1, c);
+            if (f) atomicOr(J.a.status, kStatusNonfinite), atomicOr(&J.ctl->flags, kStatusNonfinite);
+        }
+    }
+}
+
+// Encode item i of field J: scan tile ne-1-i (the last tile first: the range launch read
+// the field front to back, so its end is the part most likely still in L2), one shuffle
+// block per warp; r = ebx2_r.
+template <int ND>
+__device__ __forceinline__ void encode_item(const FieldJob& J, uint32_t i, float r, uint32_t* sm)
+{
+    const uint32_t      lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const CompressArgs& a    = J.a;
+    Geo                 g;
+    g.nl = a.nl, g.x = a.x, g.y = a.y, g.xy = a.xy, g.lim = a.n;
+    g.dx = a.dx, g.dxy = a.dxy, g.al_x = a.al_x, g.al_xy = a.al_xy, g.al_xyx = a.al_xyx;
+    uint32_t* signw = (ND == 1 && a.mode == 1) ? reinterpret_cast<uint32_t*>(a.out + a.off_sign) : nullptr;
+    const uint32_t t  = (J.ne - 1 - i) * kCompressWarps + wid;
+    uint32_t       bm[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cnt = 0, ovf = 0;
+    compute_block<ND>(a, g, t, r, lane, sm, signw, bm, cnt, ovf);  // warp-uniform t
+    if (t < a.nb) {
+        uint4*         S   = J.slots + (size_t)t * kChunks;
+        const uint32_t lt  = lanemask_lt();
+        uint32_t       pre = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) {
+            if ((bm[k] >> lane) & 1u) S[pre + __popc(bm[k] & lt)] = *reinterpret_cast<const uint4*>(sm + (lane + 32 * k) * 4);
+            pre += __popc(bm[k]);
+        }
+        if (lane == 0) {
+            J.counts[t] = cnt;
+            if (cnt) atomicAdd(J.supers + t / kSuperBlocks, cnt);
+        }
+    }
+    if (ovf && lane == 0) atomicOr(&J.ctl->flags, kCtlOverflow);
+}
+
+// Compaction item i of field J: blocks [32 i, 32 i + 32) -- offsets from the per-512-block
+// sums and the counts, the offset table, the chunks from the slots to Section B (four
+// 16-byte loads in flight per thread; output chunk q comes from the last block j with
+// pre[j] <= q); the field's last compaction item writes the header and restores the
+// field's control words.
+__device__ __forceinline__ void compact_item(const FieldJob& J, uint32_t i, uint32_t* s_red0, uint32_t* s_red1,
+                                             uint32_t* s_pre, uint32_t* s_tot, uint32_t* s_last)
+{
+    const uint32_t      tid = threadIdx.x, lane = tid & 31u, wid = tid >> 5;
+    const CompressArgs& a   = J.a;
+    const uint32_t      b0 = i * kCompactBlocks, sup = b0 / kSuperBlocks;
+    const uint32_t      c  = (wid == 0 && b0 + lane < a.nb) ? __ldcg(J.counts + b0 + lane) : 0u;
+    uint32_t            acc = 0;
+    for (uint32_t k = tid; k < sup; k += blockDim.x) acc += __ldcg(J.supers + k);
+    for (uint32_t b = sup * kSuperBlocks + tid; b < b0; b += blockDim.x) acc += __ldcg(J.counts + b);
+    const uint32_t excl = block_sum(acc, s_red0);
     if (wid == 0) {
-        const uint32_t b = b0 + lane;
-        uint32_t       v = c;
+        uint32_t v = c;
 #pragma unroll
         for (uint32_t o = 1; o < 32; o <<= 1) {
             const uint32_t u = __shfl_up_sync(kFull, v, o);
             if (lane >= o) v += u;
         }
         s_pre[lane] = v - c;
-        if (lane == 31) s_tot = v;
-        if (a.boff && b < a.nb) a.boff[b] = excl + v - c;
+        if (lane == 31) *s_tot = v;
+        if (a.boff && b0 + lane < a.nb) a.boff[b0 + lane] = excl + v - c;
     }
     __syncthreads();
-    const uint32_t tot = s_tot;
+    const uint32_t tot = *s_tot;
     uint4*         B   = reinterpret_cast<uint4*>(a.out + a.off_b) + excl;
     for (uint32_t q0 = tid; q0 < tot; q0 += 4 * 256) {
         uint4    v[4];
@@ -1082,53 +1149,103 @@ __global__ void __launch_bounds__(256) k_compact(const CompressArgs a, const uin
             const uint32_t q = q0 + u * 256;
             qq[u]            = q;
             if (q < tot) {
-                uint32_t j = 0;  // last block with pre[j] <= q (a block with no chunks never matches last)
+                uint32_t j = 0;
 #pragma unroll
                 for (uint32_t step = 16; step; step >>= 1)
                     if (s_pre[j + step] <= q) j += step;
-                v[u] = __ldcg(slots + (size_t)(b0 + j) * kChunks + (q - s_pre[j]));
+                v[u] = __ldcg(J.slots + (size_t)(b0 + j) * kChunks + (q - s_pre[j]));
             }
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u)
             if (qq[u] < tot) B[qq[u]] = v[u];
     }
-    // the last CTA to finish: header, offset-table total, resets
+    // the field's last item to finish: header, offset-table total, resets
+    __threadfence();  // this thread's stream writes before the count
     __syncthreads();
-    if (tid == 0) {
-        __threadfence();  // this CTA's reads of the sums precede its count
-        s_last = atomicAdd(done, 1u) == gridDim.x - 1;
-    }
+    if (tid == 0) *s_last = atomicAdd(&J.ctl->c_done, 1u) == J.nc - 1;
     __syncthreads();
-    if (!s_last) return;
+    if (!*s_last) return;
     __threadfence();
-    const uint32_t nsup  = (uint32_t)cdiv(a.nb, kSuperBlocks);
-    uint32_t       total = 0;
-    for (uint32_t i = tid; i < nsup; i += blockDim.x) total += __ldcg(supers + i);
-    total = block_sum(total, s_red);
-    for (uint32_t i = tid; i < nsup; i += blockDim.x) supers[i] = 0;
+    const uint32_t nsup    = (uint32_t)cdiv(a.nb, kSuperBlocks);
+    uint32_t       total_c = 0;
+    for (uint32_t k = tid; k < nsup; k += blockDim.x) total_c += __ldcg(J.supers + k);
+    total_c = block_sum(total_c, s_red1);
+    for (uint32_t k = tid; k < nsup; k += blockDim.x) J.supers[k] = 0;
     if (tid == 0) {
-        const EbInfo eb = a.mm ? eb_from_range(ord2f(__ldcg(a.mm)), ord2f(__ldcg(a.mm + 1)), a.eb_rel) : a.ebh;
-        // ovfw: bit 0 some code overflowed (k_encode), kStatusNonfinite (k_range) -- this call's own bits
-        const uint32_t cw = __ldcg(ovfw);
-        write_header(a, eb, ((cw & 1u) ? 1u : 0u) | ((cw & kStatusNonfinite) ? 2u : 0u), total);
+        FieldCtl*      C  = J.ctl;
+        const EbInfo   eb = J.rel ? eb_from_range(ord2f(__ldcg(C->mm)), ord2f(__ldcg(C->mm + 1)), a.eb_rel) : a.ebh;
+        const uint32_t cf = __ldcg(&C->flags);
+        write_header(a, eb, ((cf & kCtlOverflow) ? 1u : 0u) | ((cf & kStatusNonfinite) ? 2u : 0u), total_c);
         if (a.boff) {
-            // the total closes the offset table; zero its 16-byte pad
-            a.boff[a.nb] = total;
-            for (uint32_t i = a.nb + 1; i < (uint32_t)(pad16(4ull * (a.nb + 1)) / 4); ++i) a.boff[i] = 0;
+            a.boff[a.nb] = total_c;  // the total closes the offset table; zero its 16-byte pad
+            for (uint32_t k = a.nb + 1; k < (uint32_t)(pad16(4ull * (a.nb + 1)) / 4); ++k) a.boff[k] = 0;
         }
-        *ovfw = 0;
-        *done = 0;
-        if (a.mm) a.mm[0] = 0xFFFFFFFFu, a.mm[1] = 0u;  // empty range for the next call
+        C->mm[0] = 0xFFFFFFFFu, C->mm[1] = 0u;
+        C->c_done = 0, C->flags = 0;
         if (a.mirror) {
             // header and status in one place, so a caller reads both with one copy
             __threadfence();
             const uint4* h = reinterpret_cast<const uint4*>(a.out);
             uint4*       m = reinterpret_cast<uint4*>(a.mirror);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) m[i] = __ldcg(h + i);
+            for (int k = 0; k < 4; ++k) m[k] = __ldcg(h + k);
             a.mirror[16] = __ldcg(a.status);
         }
+    }
+}
+
+// -------------------------------------------------------------- kernels --
+// kList false: one field, `one` (a kernel parameter: its fields are constant-bank operands
+// and take no registers); true: the fields jobs[] of a batch, located through segs[].
+template <bool kList>
+__global__ void __launch_bounds__(256) k_range_fields(const FieldJob* __restrict__ jobs, const Segment* __restrict__ segs,
+                                                      uint32_t nseg, uint32_t total, const __grid_constant__ FieldJob one)
+{
+    __shared__ uint32_t s_red[3][kCompressWarps];
+    for (uint32_t k = blockIdx.x; k < total; k += gridDim.x) {
+        uint32_t f = 0, i = k;
+        if (kList) locate(segs, nseg, k, f, i);
+        range_item(kList ? jobs[f] : one, i, s_red);
+        __syncthreads();  // s_red before the next item
+    }
+}
+
+template <int ND, bool kList>
+__global__ void __launch_bounds__(kCompressWarps * 32, ND == 3 ? 4 : 5)
+    k_encode_fields(const FieldJob* __restrict__ jobs, const Segment* __restrict__ segs, uint32_t nseg, uint32_t total,
+                    const __grid_constant__ FieldJob one)
+{
+    __shared__ __align__(16) uint32_t smem[kCompressWarps][kBlockWords];
+    __shared__ float    s_r;
+    __shared__ uint32_t s_rf;
+    if (threadIdx.x == 0) s_rf = 0xFFFFFFFFu;
+    for (uint32_t k = blockIdx.x; k < total; k += gridDim.x) {
+        uint32_t f = 0, i = k;
+        if (kList) locate(segs, nseg, k, f, i);
+        const FieldJob& J = kList ? jobs[f] : one;
+        if (threadIdx.x == 0 && s_rf != f) {
+            // ebx2_r of the field: from its range (relative eb; the range launch has finished)
+            s_r  = J.rel ? eb_from_range(ord2f(__ldcg(J.ctl->mm)), ord2f(__ldcg(J.ctl->mm + 1)), J.a.eb_rel).ebx2_r
+                         : J.a.ebh.ebx2_r;
+            s_rf = f;
+        }
+        __syncthreads();
+        encode_item<ND>(J, i, s_r, smem[threadIdx.x >> 5]);
+        __syncthreads();  // the blocks' shared images before the next item
+    }
+}
+
+template <bool kList>
+__global__ void __launch_bounds__(256) k_compact_fields(const FieldJob* __restrict__ jobs, const Segment* __restrict__ segs,
+                                                        uint32_t nseg, uint32_t total, const __grid_constant__ FieldJob one)
+{
+    __shared__ uint32_t s_red[2][kCompressWarps], s_pre[kCompactBlocks], s_tot, s_last;
+    for (uint32_t k = blockIdx.x; k < total; k += gridDim.x) {
+        uint32_t f = 0, i = k;
+        if (kList) locate(segs, nseg, k, f, i);
+        compact_item(kList ? jobs[f] : one, i, s_red[0], s_red[1], s_pre, &s_tot, &s_last);
+        __syncthreads();
     }
 }
 
@@ -1173,23 +1290,68 @@ cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* st
     return cudaGetLastError();
 }
 
-cudaError_t launch_encode(const CompressArgs& a, uint4* slots, uint32_t* counts, uint32_t* supers, uint32_t* ovfw,
-                          cudaStream_t s)
+
+
+
+
+
+// Resident CTAs of each list-compression kernel on the current device, cached per device
+// (ordinals below 64): [0] range, [1..3] encode<1..3>, [4] compaction.
+static uint32_t list_wave(int which, bool list)
 {
-    const uint32_t ctas = (uint32_t)cdiv(a.ntiles, kCompressWarps);
-    switch (a.ndim) {
-    case 1: k_encode<1><<<ctas, kCompressWarps * 32, 0, s>>>(a, slots, counts, supers, ovfw); break;
-    case 2: k_encode<2><<<ctas, kCompressWarps * 32, 0, s>>>(a, slots, counts, supers, ovfw); break;
-    default: k_encode<3><<<ctas, kCompressWarps * 32, 0, s>>>(a, slots, counts, supers, ovfw); break;
+    static std::atomic<uint32_t> cache[64][2][5];
+    int                          dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    std::atomic<uint32_t>* slot = (dev >= 0 && dev < 64) ? &cache[dev][list ? 1 : 0][which] : nullptr;
+    uint32_t               w    = slot ? slot->load(std::memory_order_acquire) : 0u;
+    if (w) return w;
+    constexpr int T = kCompressWarps * 32;
+    if (list) {
+        w = which == 0 ? resident_ctas(k_range_fields<true>, T)
+            : which == 1 ? resident_ctas(k_encode_fields<1, true>, T)
+            : which == 2 ? resident_ctas(k_encode_fields<2, true>, T)
+            : which == 3 ? resident_ctas(k_encode_fields<3, true>, T)
+                         : resident_ctas(k_compact_fields<true>, T);
+    } else {
+        w = which == 0 ? resident_ctas(k_range_fields<false>, T)
+            : which == 1 ? resident_ctas(k_encode_fields<1, false>, T)
+            : which == 2 ? resident_ctas(k_encode_fields<2, false>, T)
+            : which == 3 ? resident_ctas(k_encode_fields<3, false>, T)
+                         : resident_ctas(k_compact_fields<false>, T);
     }
-    return cudaGetLastError();
+    if (slot) slot->store(w, std::memory_order_release);
+    return w;
 }
 
-cudaError_t launch_compact(const CompressArgs& a, const uint4* slots, const uint32_t* counts, uint32_t* supers,
-                           uint32_t* ovfw, uint32_t* done, cudaStream_t s)
+cudaError_t launch_fields(FieldPhase phase, int nd, const FieldJob* jobs, const Segment* segs, uint32_t nseg,
+                          uint32_t total, const FieldJob& one, cudaStream_t s)
 {
-    const uint32_t ctas = (uint32_t)std::max<uint64_t>(1, cdiv(a.nb, kCompactBlocks));
-    k_compact<<<ctas, 256, 0, s>>>(a, slots, counts, supers, ovfw, done);
+    if (!total) return cudaSuccess;
+    const bool list = jobs != nullptr;
+    if (list && (!segs || !nseg)) return cudaErrorInvalidValue;
+    const int      which = phase == FieldPhase::Range ? 0 : phase == FieldPhase::Encode ? nd : 4;
+    const uint32_t wave  = list_wave(which, list);
+    if (!wave) return cudaErrorInvalidDevice;
+    const dim3 grid(std::min(total, wave)), block(kCompressWarps * 32);
+    if (phase == FieldPhase::Range) {
+        if (list) k_range_fields<true><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one);
+        else k_range_fields<false><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one);
+    } else if (phase == FieldPhase::Compact) {
+        if (list) k_compact_fields<true><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one);
+        else k_compact_fields<false><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one);
+    } else if (list) {
+        switch (nd) {
+        case 1: k_encode_fields<1, true><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one); break;
+        case 2: k_encode_fields<2, true><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one); break;
+        default: k_encode_fields<3, true><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one); break;
+        }
+    } else {
+        switch (nd) {
+        case 1: k_encode_fields<1, false><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one); break;
+        case 2: k_encode_fields<2, false><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one); break;
+        default: k_encode_fields<3, false><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one); break;
+        }
+    }
     return cudaGetLastError();
 }
 

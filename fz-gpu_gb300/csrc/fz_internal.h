@@ -49,9 +49,54 @@ struct CompressArgs {
     uint32_t*    status;
     uint32_t*    epoch;  // device epoch word (advanced by the kernel's last ticket fetch)
     uint32_t*    boff;   // block offset table in the stream's sidecar, or null
-    uint32_t*    mirror; // k_compact: 64-byte header + status word copied here, or null
+    uint32_t*    mirror; // list compression: 64-byte header + status word copied here, or null
     uint32_t*    fin;    // k_compress: CTA exit counter (zero on entry, left zero), or null
 };
+
+// ------------------------------------------------------ list compression --
+// Compression of a list of fields in three launches (range, encode per dimensionality,
+// compaction), each a persistent grid striding over the list's items: range items (a
+// 16384-element chunk's max/min, relative eb only), encode items (8 shuffle blocks:
+// codes, bitshuffle, flags, chunks into per-block slots) and compaction items (32 blocks:
+// offsets, chunks to their final place; a field's last one writes its header).  One field
+// is a list of one, passed as a kernel parameter.
+
+// Per-field control words (device, 32 bytes).  Between calls: mm = {0xFFFFFFFF, 0}, the
+// rest 0 -- the field's last compaction item restores that.
+struct FieldCtl {
+    uint32_t mm[2];    // range accumulators (order-preserving u32)
+    uint32_t c_done;   // finished compaction items
+    uint32_t flags;    // this call: kStatusNonfinite, bit 8 code overflow
+    uint32_t pad[4];
+};
+
+struct FieldJob {
+    CompressArgs a;       // geometry, stream offsets, eb (a.mm unused), status, boff, mirror
+    FieldCtl*    ctl;
+    uint4*       slots;   // 4 KiB per shuffle block
+    uint32_t*    counts;  // chunks per block
+    uint32_t*    supers;  // chunks per 512 blocks (zero on entry, left zero)
+    uint32_t     nr, ne, nc;  // range, encode, compaction items
+    uint32_t     rel;         // relative eb: the eb follows from the range items
+};
+
+// Items [start, start + count) of a list launch belong to field `field` (its items 0 ..
+// count-1 of that launch's kind); segments sorted by start, no gaps.
+struct Segment {
+    uint32_t start, field, count, pad;
+};
+
+enum class FieldPhase { Range, Encode, Compact };
+
+constexpr uint32_t kSuperBlocks = 512;  // shuffle blocks per group sum of chunk counts
+
+// Items of each kind for a field of n elements (ntiles scan tiles of shuffle blocks, nb full
+// blocks).
+void field_items(uint32_t n, uint32_t nb, uint32_t ntiles, bool rel, uint32_t& nr, uint32_t& ne, uint32_t& nc);
+// One list launch of `phase` (encode: of dimensionality nd) over `total` items: jobs/segs
+// device arrays of a batch, or jobs == nullptr and `one` the only field.
+cudaError_t launch_fields(FieldPhase phase, int nd, const FieldJob* jobs, const Segment* segs, uint32_t nseg,
+                          uint32_t total, const FieldJob& one, cudaStream_t s);
 
 struct DecodeArgs {
     const uint8_t*  st;
@@ -77,12 +122,6 @@ struct ReconArgs {
 cudaError_t launch_range(const float* in, uint32_t n, uint32_t* mm, uint32_t* status, uint32_t* callw,
                          cudaStream_t s);
 cudaError_t launch_compress(const CompressArgs& a, cudaStream_t s);  // fused, single launch
-// two launches with per-block slots in a scratch of 4 KiB per shuffle block (workspace path);
-// supers: chunk counts per 512 blocks (zero on entry, left zero), done: a zero word
-cudaError_t launch_encode(const CompressArgs& a, uint4* slots, uint32_t* counts, uint32_t* supers, uint32_t* ovfw,
-                          cudaStream_t s);
-cudaError_t launch_compact(const CompressArgs& a, const uint4* slots, const uint32_t* counts, uint32_t* supers,
-                           uint32_t* ovfw, uint32_t* done, cudaStream_t s);
 cudaError_t launch_offsets(const uint8_t* st, uint64_t off_a, uint32_t nb, uint32_t nwords, uint64_t nnz,
                            uint32_t* boff, uint64_t* state, uint32_t* ticket, uint32_t* status,
                            uint32_t* epoch, cudaStream_t s);

@@ -13,13 +13,14 @@ struct fz_workspace {
     void*     d_base;
     size_t    d_bytes;
     uint64_t* state;
-    uint32_t* tickets;  // [0] compress, [1] offsets, [2] scan-encode
+    uint32_t* tickets;  // [0] look-back compress, [1] offsets, [2] scan-encode, [3] unused
     uint32_t* status;
     uint32_t* total;
     uint32_t* epoch;    // device epoch of the scan state
     uint32_t* ovfw;     // overflow bits of the two-launch compression (reset by k_compact)
     uint32_t* done;     // k_compact CTAs finished (the last one resets it)
-    uint32_t* supers;   // chunk counts per 512 shuffle blocks (two-launch compression)
+    uint32_t* supers;   // chunk counts per 512 shuffle blocks
+    fz::FieldCtl* fctl; // control words of the list compression
     uint32_t* mm;       // range accumulators (min, max as ordered u32)
     uint16_t* codes;
     uint32_t* boff;     // chunk offset of each shuffle block (decompression)

@@ -153,10 +153,11 @@ fz_status fz_workspace_status(fz_workspace* ws, fz_stream_t stream);
    by a call on this workspace (up to `capacity` launches in total) is bracketed by a
    pair of CUDA events on the call's stream.  capacity 0 disables it. */
 fz_status fz_workspace_enable_timing(fz_workspace* ws, uint32_t capacity);
-/* Number of recorded launches of one kernel kind (0 range pass, 1 compress -- codes,
-   bitshuffle, flags and per-block compaction --, 2 block offsets, 3 decode -- fused with
-   the inverse Lorenzo --, 4 separate inverse Lorenzo, 5 compaction scan and move) and
-   their summed duration; syncs on the last recorded event and frees those records. */
+/* Number of recorded launches of one kernel kind (0 range pass, 1 encode -- codes,
+   bitshuffle, flags and per-block compaction into slots --, 2 block offsets, 3 decode --
+   fused with the inverse Lorenzo --, 4 separate inverse Lorenzo, 5 compaction -- offsets
+   and the move into the stream) and their summed duration; syncs on the last recorded
+   event and frees those records. */
 fz_status fz_workspace_kernel_time(fz_workspace* ws, int kind, uint32_t* launches,
                                    double* total_ms);
 
@@ -303,6 +304,28 @@ fz_status fz_batch_create_ex(fz_workspace* ws, const fz_field* fields, uint32_t 
    streams, so the captured headers stay valid. */
 fz_status fz_batch_create_pair(fz_workspace* ws, const fz_field* comp, const fz_field* dec, uint32_t count,
                                fz_eb_mode eb_mode, fz_mode mode, uint32_t branches, fz_batch** out);
+
+/* Batch schedules (no counterpart in the reference).  branches: parallel graph branches
+   for per-field work (1..FZ_BATCH_MAX_BRANCHES, 0 = 8).  list = 1: the compression of every
+   field as list launches -- one range launch, one encode launch per dimensionality present
+   and one compaction launch, persistent grids striding over a device work list of all the
+   batch's fields (per-field jobs, control words and slots allocated with the batch, 2
+   bytes per element) -- and decompressions, if any, on the branches after it; list = 0:
+   each field's compression (and decompression) on its branch.  comp and dec may each be
+   NULL (not both); with both, dec[i] decompresses what comp[i] compresses. */
+typedef struct fz_batch_schedule {
+    uint32_t branches;
+    uint32_t list;
+} fz_batch_schedule;
+fz_status fz_batch_create_sched(fz_workspace* ws, const fz_field* comp, const fz_field* dec, uint32_t count,
+                                fz_eb_mode eb_mode, fz_mode mode, const fz_batch_schedule* sched, fz_batch** out);
+/* Times every schedule (branches 1, 2, 4, 8, 16 capped at count, each with list 0 and 1)
+   on these fields, `reps` replays each on `stream`, and returns the fastest in *best; ms
+   (nullable) receives the mean replay times, ms[0..4] list 0 and ms[5..9] list 1 (0 for
+   candidates not run). */
+fz_status fz_batch_autotune_sched(fz_workspace* ws, const fz_field* comp, const fz_field* dec, uint32_t count,
+                                  fz_eb_mode eb_mode, fz_mode mode, uint32_t reps, fz_stream_t stream,
+                                  fz_batch_schedule* best, double* ms);
 
 /* Autotuner for batch scheduling (no counterpart in the reference).  The stream format
    fixes the shuffle block and the Lorenzo tiles, so what is tuned is how many fields run

@@ -36,8 +36,12 @@ def test_slice_covers_the_mix(fz, batch_slice):
     assert any(fz.ndim(dims) > 1 and dims[0] % 4 for _, _, dims, _ in items)
 
 
-@pytest.mark.parametrize("branches", [0, 16])
-def test_pair_batch_matches_oracle_at_scale(fz, oracle, batch_slice, branches):
+@pytest.mark.parametrize("branches,listed", [(0, 0), (16, 0), (8, 1)])
+def test_pair_batch_matches_oracle_at_scale(fz, oracle, batch_slice, branches, listed):
+    """Round trips of the slice under each schedule: per-field launches on 8 or 16 graph
+    branches, or the compression of all 32 fields as list launches (one range launch, one
+    encode launch per dimensionality, one compaction launch over a device work list), each
+    replayed twice."""
     items, wants = batch_slice
     ws = fz.Workspace(max(d.size for _, d, _, _ in items))
     xs = [torch.from_numpy(d).cuda() for _, d, _, _ in items]
@@ -48,14 +52,17 @@ def test_pair_batch_matches_oracle_at_scale(fz, oracle, batch_slice, branches):
                              "dst_capacity": s.numel()} for x, s, (_, _, dims, eb) in zip(xs, ss, items)])
     dec = fz.fields_array([{"src": s.data_ptr(), "dst": y.data_ptr(), "src_bytes": w.size, "dst_capacity": y.numel(),
                             "header": fz.parse_header(w)} for s, y, w in zip(ss, ys, wants)])
-    g = fz.Batch.pair(ws, comp, dec, branches=branches)
-    g.launch()
-    torch.cuda.synchronize()
-    for (i, d, dims, eb), s, y, w in zip(items, ss, ys, wants):
-        got = s[: w.size].cpu().numpy()
-        bad = np.nonzero(got != w)[0]
-        assert bad.size == 0, f"field {i} {dims} eb={eb}: {bad.size} stream bytes differ, first at {bad[:4]}"
-        rec = y.cpu().numpy()
-        assert np.array_equal(rec.view(np.uint32), oracle.decompress(w).view(np.uint32)), f"field {i} {dims}"
+    g = fz.Batch.scheduled(ws, comp, dec, fz.Schedule(branches, listed))
+    for rep in range(2):
+        for s in ss:
+            s.fill_(0xA5 + rep)
+        g.launch()
+        torch.cuda.synchronize()
+        for (i, d, dims, eb), s, y, w in zip(items, ss, ys, wants):
+            got = s[: w.size].cpu().numpy()
+            bad = np.nonzero(got != w)[0]
+            assert bad.size == 0, f"field {i} {dims} eb={eb}: {bad.size} stream bytes differ, first at {bad[:4]}"
+            rec = y.cpu().numpy()
+            assert np.array_equal(rec.view(np.uint32), oracle.decompress(w).view(np.uint32)), f"field {i} {dims}"
     g.close()
     assert ws.status() == fz.SUCCESS

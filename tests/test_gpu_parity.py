@@ -436,6 +436,40 @@ def test_compaction_group_boundaries(fz, oracle, ws, nblocks, extra):
         assert np.array_equal(rec.view(np.uint32), oracle.decompress(want).view(np.uint32))
 
 
+def test_list_schedule_batches_and_autotune(fz, oracle, synth):
+    """Compression as list launches over all fields (fz_batch_create_sched, list = 1):
+    compress-only and round-trip batches, replayed three times (the per-field control words
+    and group sums are restored by each replay's last compaction item), equal the oracle;
+    the schedule autotuner times both kinds of schedule and returns one of them."""
+    items = _mixed_fields(synth) + [(synth.smooth2d(130, 9, seed=26), (130, 9, 1), 1e-3),
+                                    (synth.smooth1d(1500, seed=27), (1500, 1, 1), 1e-2)]
+    ws = fz.Workspace(max(d.size for d, _, _ in items))
+    xs, ss, ys, comp = _batch_buffers(fz, items)
+    wants = [oracle.compress(d, dims, eb) for d, dims, eb in items]
+    dec = fz.fields_array([{"src": s.data_ptr(), "dst": y.data_ptr(), "src_bytes": w.size, "dst_capacity": y.numel(),
+                            "header": fz.parse_header(w)} for s, y, w in zip(ss, ys, wants)])
+    for pair in (False, True):
+        g = fz.Batch.scheduled(ws, comp, dec if pair else None, fz.Schedule(4, 1))
+        for _ in range(3):
+            for s in ss:
+                s.fill_(0x3C)
+            for y in ys:
+                y.fill_(9.0)
+            g.launch()
+            torch.cuda.synchronize()
+            for s, y, w in zip(ss, ys, wants):
+                assert_same_stream(s[: w.size].cpu().numpy(), w)
+                if pair:
+                    assert np.array_equal(y.cpu().numpy().view(np.uint32), oracle.decompress(w).view(np.uint32))
+        g.close()
+    best, ms = fz.batch_autotune_schedule(ws, comp, dec, reps=2)
+    assert (best.branches, best.list) in ms and (1, 1) in ms and (1, 0) in ms
+    torch.cuda.synchronize()
+    for s, w in zip(ss, wants):
+        assert_same_stream(s[: w.size].cpu().numpy(), w)
+    assert ws.status() == fz.SUCCESS
+
+
 def test_round_trip_pair_batch(fz, oracle, synth):
     """fz_batch_create_pair: each field compressed then decompressed on one branch of one
     graph; every replay reproduces the oracle's streams and reconstructions."""
