@@ -23,6 +23,19 @@
 
 #include "fz_internal.h"
 
+#ifndef FZ_ENCODE_RING
+#define FZ_ENCODE_RING 4
+#endif
+#ifndef FZ_RANGE_VEC
+#define FZ_RANGE_VEC 8
+#endif
+#ifndef FZ_RANGE_ROUNDS
+#define FZ_RANGE_ROUNDS 2
+#endif
+#ifndef FZ_ENCODE_CTAS
+#define FZ_ENCODE_CTAS 3
+#endif
+
 namespace fz {
 
 __device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
@@ -267,6 +280,138 @@ __device__ __forceinline__ void block1d(const float* __restrict__ in, uint32_t b
             if ((lane & 7u) == 0) signw[(base >> 5) + it * 4 + (lane >> 3)] = sv;
         }
         v = vn;
+        e0 += 128;
+    }
+    ovf |= (!(amax0 < 32768.0f) || !(amax1 < 65536.0f)) ? 1u : 0u;
+}
+
+// ------------------------------------------------- asynchronous row ring --
+// The whole-block paths below keep kRing group rows of input in flight per warp without
+// holding them in registers: every lane copies its own 16-byte pieces (its 4 elements of
+// the centre row and of the north row) into a per-warp ring in shared memory with
+// cp.async, kRing group rows ahead, and waits only for its own copies (cp.async.wait_group),
+// so no lane waits for another.  A north row outside the element's tile is zero-filled
+// (source size 0) instead of read.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// block2d with the ring: the same float expressions, positions and carried west values;
+// group row it's inputs come from ring slot it % kRing, refilled with group row it + kRing
+// once they have been used.
+template <int kRing>
+__device__ __forceinline__ void block2d_ring(const float* __restrict__ in, const Geo& g, uint32_t base, float r,
+                                             uint32_t lane, uint32_t* sm, float4* ring, uint32_t& ovf)
+{
+    static_assert(kRing >= 2 && 4 % kRing == 0, "slot of an unrolled row is a constant");
+    uint32_t       e0 = base + lane * 4;
+    uint32_t       row0 = fdiv(e0, g.dx), col0 = e0 - row0 * g.x;  // group row being computed
+    uint32_t       ei = e0, rowi = row0, coli = col0;              // group row being fetched
+    const uint32_t rs = (uint32_t)__cvta_generic_to_shared(ring) + lane * 16;
+#pragma unroll
+    for (int k = 0; k < kRing; ++k) {
+        const bool nin = (rowi & 15u) != 0;
+        cp_async16(rs + k * 1024, in + ei, 16);
+        cp_async16(rs + k * 1024 + 512, nin ? in + (ei - g.x) : in + ei, nin ? 16u : 0u);
+        cp_async_commit();
+        advance128(g, ei, rowi, coli);
+        ei += 128;
+    }
+    // t = c - n of element base-1, the west neighbour of lane 0's first group
+    float carry = 0.0f;
+    if (lane == 0 && (col0 & 15u))
+        carry = __fsub_rn(pq(__ldg(in + e0 - 1), r), (row0 & 15u) ? pq(__ldg(in + e0 - 1 - g.x), r) : 0.0f);
+    SwzRot         so(lane);
+    const uint32_t prev = (lane + 31u) & 31u;
+    float          amax = 0.0f;
+#pragma unroll 4
+    for (uint32_t it = 0; it < 16; ++it) {
+        cp_async_wait<kRing - 1>();  // this lane's copies of group row it have landed
+        const float4* slot = ring + (it % kRing) * 64 + lane;
+        const float4  v0 = slot[0], u0 = slot[32];
+        const bool    cin = (col0 & 15u) != 0;
+        float         t[4];
+        t[0] = __fsub_rn(pq(v0.x, r), pq(u0.x, r));
+        t[1] = __fsub_rn(pq(v0.y, r), pq(u0.y, r));
+        t[2] = __fsub_rn(pq(v0.z, r), pq(u0.z, r));
+        t[3] = __fsub_rn(pq(v0.w, r), pq(u0.w, r));
+        const float rot = __shfl_sync(kFull, t[3], prev);
+        const float tw  = cin ? (lane ? rot : carry) : 0.0f;
+        carry           = rot;
+        float d[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) d[j] = __fsub_rn(t[j], j ? t[j - 1] : tw);
+        amax = fmax3_nan(amax, fabsf(d[0]), fabsf(d[1]));
+        amax = fmax3_nan(amax, fabsf(d[2]), fabsf(d[3]));
+        *reinterpret_cast<uint2*>(sm + it * 64 + so.x0) =
+            make_uint2(pack_signed_pair(d[0], d[1]), pack_signed_pair(d[2], d[3]));
+        so.next();
+        if (it + kRing < 16) {  // the slot's values are in registers and used: refill it
+            const bool     nin = (rowi & 15u) != 0;
+            const uint32_t dst = rs + (it % kRing) * 1024;
+            cp_async16(dst, in + ei, 16);
+            cp_async16(dst + 512, nin ? in + (ei - g.x) : in + ei, nin ? 16u : 0u);
+            advance128(g, ei, rowi, coli);
+            ei += 128;
+        }
+        cp_async_commit();  // (empty in the last rows: keeps the group count per row)
+        advance128(g, e0, row0, col0);
+        e0 += 128;
+    }
+    ovf |= !(amax < 32768.0f) ? 1u : 0u;
+}
+
+// block1d with the ring (centre rows only).
+template <int kRing>
+__device__ __forceinline__ void block1d_ring(const float* __restrict__ in, uint32_t base, float r, uint32_t lane,
+                                             uint32_t* sm, uint32_t* signw, float4* ring, uint32_t& ovf)
+{
+    static_assert(kRing >= 2 && 4 % kRing == 0, "slot of an unrolled row is a constant");
+    uint32_t       e0 = base + lane * 4;
+    const uint32_t rs = (uint32_t)__cvta_generic_to_shared(ring) + lane * 16;
+#pragma unroll
+    for (int k = 0; k < kRing; ++k) {
+        cp_async16(rs + k * 1024, in + e0 + 128 * k, 16);
+        cp_async_commit();
+    }
+    float          carry = 0.0f;
+    float          amax0 = 0.0f, amax1 = 0.0f;
+    SwzRot         so(lane);
+    const uint32_t prev = (lane + 31u) & 31u;
+#pragma unroll 4
+    for (uint32_t it = 0; it < 16; ++it) {
+        cp_async_wait<kRing - 1>();
+        const float4 v  = ring[(it % kRing) * 64 + lane];
+        const float  p0 = pq(v.x, r), p1 = pq(v.y, r), p2 = pq(v.z, r), p3 = pq(v.w, r);
+        const float  rot = __shfl_sync(kFull, p3, prev);
+        const float  w   = (e0 & 255u) ? (lane ? rot : carry) : 0.0f;
+        carry            = rot;
+        const float d0 = __fsub_rn(p0, w), d1 = __fsub_rn(p1, p0), d2 = __fsub_rn(p2, p1), d3 = __fsub_rn(p3, p2);
+        amax0          = fmax_nan(amax0, fabsf(d0));
+        amax1          = fmax_nan(amax1, fmax3_nan(fabsf(d1), fabsf(d2), fabsf(d3)));
+        const uint32_t m0 = static_cast<uint32_t>(fabsf(d0)), m1 = static_cast<uint32_t>(fabsf(d1));
+        const uint32_t m2 = static_cast<uint32_t>(fabsf(d2)), m3 = static_cast<uint32_t>(fabsf(d3));
+        *reinterpret_cast<uint2*>(sm + it * 64 + so.x0) =
+            make_uint2(__byte_perm(m0, m1, 0x5410) | (d0 < 0.0f ? 0x8000u : 0u), __byte_perm(m2, m3, 0x5410));
+        so.next();
+        if (signw) {
+            const uint32_t sgn = (d0 < 0.0f ? 1u : 0u) | (d1 < 0.0f ? 2u : 0u) | (d2 < 0.0f ? 4u : 0u) |
+                                 (d3 < 0.0f ? 8u : 0u);
+            uint32_t sv = sgn << ((lane & 7u) * 4);
+            sv |= __shfl_xor_sync(kFull, sv, 1);
+            sv |= __shfl_xor_sync(kFull, sv, 2);
+            sv |= __shfl_xor_sync(kFull, sv, 4);
+            if ((lane & 7u) == 0) signw[(base >> 5) + it * 4 + (lane >> 3)] = sv;
+        }
+        if (it + kRing < 16) cp_async16(rs + (it % kRing) * 1024, in + e0 + 128 * kRing, 16);
+        cp_async_commit();
         e0 += 128;
     }
     ovf |= (!(amax0 < 32768.0f) || !(amax1 < 65536.0f)) ? 1u : 0u;
@@ -740,18 +885,23 @@ __device__ void write_header(const CompressArgs& a, const EbInfo& e, uint32_t fl
 // as 8 ballots (= bitmap words 8t..8t+7, stored), the chunk count and the overflow bit.
 // Block t == nb (the n mod 2048 tail, never shuffled, fz.cu:173) writes its codes to the
 // sidecar and zero-fills the 16-byte pads of Sections A and C.
-template <int ND>
+// kRing > 0: the aligned 1D/2D whole-block paths take their inputs through a cp.async ring
+// of kRing group rows at `ring` (1 KiB per group row and warp).
+template <int ND, int kRing = 0>
 __device__ __forceinline__ void compute_block(const CompressArgs& a, const Geo& g, uint32_t t, float r,
                                               uint32_t lane, uint32_t* sm, uint32_t* signw,
-                                              uint32_t (&bm)[8], uint32_t& cnt, uint32_t& ovf)
+                                              uint32_t (&bm)[8], uint32_t& cnt, uint32_t& ovf,
+                                              float4* ring = nullptr)
 {
     const uint32_t base = t * kBlockCodes;
     if (t < a.nb) {
         // ---- phase A: codes of the block into shared memory (swizzled) ----
         if (ND == 1 && base + kBlockCodes <= g.nl) {
-            block1d(a.in, base, r, lane, sm, signw, ovf);
+            if constexpr (kRing > 0) block1d_ring<kRing>(a.in, base, r, lane, sm, signw, ring, ovf);
+            else block1d(a.in, base, r, lane, sm, signw, ovf);
         } else if (ND == 2 && g.al_x && base + kBlockCodes <= g.nl) {
-            block2d(a.in, g, base, r, lane, sm, ovf);
+            if constexpr (kRing > 0) block2d_ring<kRing>(a.in, g, base, r, lane, sm, ring, ovf);
+            else block2d(a.in, g, base, r, lane, sm, ovf);
         } else if (ND == 2 && g.x >= 4 && base + kBlockCodes <= g.nl) {
             block2d_u(a.in, g, base, r, lane, sm, ovf);
         } else if (ND == 3 && g.al_x && base + kBlockCodes <= g.nl) {
@@ -991,6 +1141,8 @@ __global__ void __launch_bounds__(kCompressWarps * 32, 3) k_compress(const Compr
 // A single field is a list of one whose job is a kernel parameter.  The stream bytes equal
 // the single-pass look-back kernel's.
 constexpr uint32_t kCompactBlocks = 32;   // shuffle blocks per compaction item
+constexpr int      kEncodeRing    = FZ_ENCODE_RING;  // group rows in flight per warp (1D/2D)
+constexpr int      kEncodeCtas    = FZ_ENCODE_CTAS;  // CTAs per SM the 1D/2D encode kernels are built for
 
 // Sum of v over the CTA (256 threads), in every thread.
 __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red)
@@ -1004,8 +1156,8 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red)
 
 // ---------------------------------------------------------------- items --
 constexpr uint32_t kCtlOverflow    = 1u << 8;                    // FieldCtl::flags: some code overflowed
-constexpr uint32_t kRangeVec       = 8;                          // 16-byte loads in flight per thread
-constexpr uint32_t kRangeRounds    = 2;                          // rounds per range item
+constexpr uint32_t kRangeVec       = FZ_RANGE_VEC;               // 16-byte loads in flight per thread
+constexpr uint32_t kRangeRounds    = FZ_RANGE_ROUNDS;            // rounds per range item
 constexpr uint32_t kRangeItemElems = 256 * kRangeVec * 4 * kRangeRounds;  // 16384
 
 void field_items(uint32_t n, uint32_t nb, uint32_t ntiles, bool rel, uint32_t& nr, uint32_t& ne, uint32_t& nc)
@@ -1082,8 +1234,8 @@ __device__ __forceinline__ void range_item(const FieldJob& J, uint32_t i, uint32
 // Encode item i of field J: scan tile ne-1-i (the last tile first: the range launch read
 // the field front to back, so its end is the part most likely still in L2), one shuffle
 // block per warp; r = ebx2_r.
-template <int ND>
-__device__ __forceinline__ void encode_item(const FieldJob& J, uint32_t i, float r, uint32_t* sm)
+template <int ND, int kRing>
+__device__ __forceinline__ void encode_item(const FieldJob& J, uint32_t i, float r, uint32_t* sm, float4* ring)
 {
     const uint32_t      lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     const CompressArgs& a    = J.a;
@@ -1093,7 +1245,7 @@ __device__ __forceinline__ void encode_item(const FieldJob& J, uint32_t i, float
     uint32_t* signw = (ND == 1 && a.mode == 1) ? reinterpret_cast<uint32_t*>(a.out + a.off_sign) : nullptr;
     const uint32_t t  = (J.ne - 1 - i) * kCompressWarps + wid;
     uint32_t       bm[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cnt = 0, ovf = 0;
-    compute_block<ND>(a, g, t, r, lane, sm, signw, bm, cnt, ovf);  // warp-uniform t
+    compute_block<ND, kRing>(a, g, t, r, lane, sm, signw, bm, cnt, ovf, ring);  // warp-uniform t
     if (t < a.nb) {
         uint4*         S   = J.slots + (size_t)t * kChunks;
         const uint32_t lt  = lanemask_lt();
@@ -1111,62 +1263,61 @@ __device__ __forceinline__ void encode_item(const FieldJob& J, uint32_t i, float
     if (ovf && lane == 0) atomicOr(&J.ctl->flags, kCtlOverflow);
 }
 
-// Compaction item i of field J: blocks [32 i, 32 i + 32) -- offsets from the per-512-block
-// sums and the counts, the offset table, the chunks from the slots to Section B (four
-// 16-byte loads in flight per thread; output chunk q comes from the last block j with
-// pre[j] <= q); the field's last compaction item writes the header and restores the
-// field's control words.
-__device__ __forceinline__ void compact_item(const FieldJob& J, uint32_t i, uint32_t* s_red0, uint32_t* s_red1,
-                                             uint32_t* s_pre, uint32_t* s_tot, uint32_t* s_last)
+// Compaction item i of field J: blocks [32 i, 32 i + 32), four per warp, each warp on its
+// own (no CTA barrier until the item's end).  A warp's first chunk offset is the sum of
+// the group sums (512 blocks each) before its group plus the counts of the blocks of its
+// group before its own; then it writes the offset table entries of its 4 blocks and moves
+// their chunks from the slots to Section B (output chunk q of the warp comes from the last
+// of its blocks whose prefix is <= q; 16-byte loads, four in flight per lane).  The field's
+// last item to finish writes the header and restores the field's control words.  No other
+// CTA reads what a compaction CTA writes, so the items need no memory fences.
+constexpr uint32_t kCompactWarpBlocks = kCompactBlocks / kCompressWarps;  // 4
+
+__device__ __forceinline__ void compact_item(const FieldJob& J, uint32_t i, uint32_t* s_red1, uint32_t* s_last)
 {
     const uint32_t      tid = threadIdx.x, lane = tid & 31u, wid = tid >> 5;
     const CompressArgs& a   = J.a;
-    const uint32_t      b0 = i * kCompactBlocks, sup = b0 / kSuperBlocks;
-    const uint32_t      c  = (wid == 0 && b0 + lane < a.nb) ? __ldcg(J.counts + b0 + lane) : 0u;
-    uint32_t            acc = 0;
-    for (uint32_t k = tid; k < sup; k += blockDim.x) acc += __ldcg(J.supers + k);
-    for (uint32_t b = sup * kSuperBlocks + tid; b < b0; b += blockDim.x) acc += __ldcg(J.counts + b);
-    const uint32_t excl = block_sum(acc, s_red0);
-    if (wid == 0) {
+    const uint32_t      b0  = i * kCompactBlocks + wid * kCompactWarpBlocks, sup = b0 / kSuperBlocks;
+    if (b0 < a.nb) {
+        uint32_t acc = 0;
+        for (uint32_t k = lane; k < sup; k += 32) acc += __ldcg(J.supers + k);
+#pragma unroll 4
+        for (uint32_t b = sup * kSuperBlocks + lane; b < b0; b += 32) acc += __ldcg(J.counts + b);
+        const uint32_t c   = lane < kCompactWarpBlocks && b0 + lane < a.nb ? __ldcg(J.counts + b0 + lane) : 0u;
+        const uint32_t exc = __reduce_add_sync(kFull, acc);
+        // inclusive prefix of the 4 counts in lanes 0..3
         uint32_t v = c;
 #pragma unroll
-        for (uint32_t o = 1; o < 32; o <<= 1) {
+        for (uint32_t o = 1; o < kCompactWarpBlocks; o <<= 1) {
             const uint32_t u = __shfl_up_sync(kFull, v, o);
             if (lane >= o) v += u;
         }
-        s_pre[lane] = v - c;
-        if (lane == 31) *s_tot = v;
-        if (a.boff && b0 + lane < a.nb) a.boff[b0 + lane] = excl + v - c;
-    }
-    __syncthreads();
-    const uint32_t tot = *s_tot;
-    uint4*         B   = reinterpret_cast<uint4*>(a.out + a.off_b) + excl;
-    for (uint32_t q0 = tid; q0 < tot; q0 += 4 * 256) {
-        uint4    v[4];
-        uint32_t qq[4];
+        if (a.boff && lane < kCompactWarpBlocks && b0 + lane < a.nb) a.boff[b0 + lane] = exc + v - c;
+        const uint32_t p1 = __shfl_sync(kFull, v - c, 1), p2 = __shfl_sync(kFull, v - c, 2);
+        const uint32_t p3 = __shfl_sync(kFull, v - c, 3), tot = __shfl_sync(kFull, v, 3);
+        uint4*         B  = reinterpret_cast<uint4*>(a.out + a.off_b) + exc;
+        for (uint32_t q0 = lane; q0 < tot; q0 += 4 * 32) {
+            uint4 val[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const uint32_t q = q0 + u * 256;
-            qq[u]            = q;
-            if (q < tot) {
-                uint32_t j = 0;
-#pragma unroll
-                for (uint32_t step = 16; step; step >>= 1)
-                    if (s_pre[j + step] <= q) j += step;
-                v[u] = __ldcg(J.slots + (size_t)(b0 + j) * kChunks + (q - s_pre[j]));
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t q = q0 + u * 32;
+                if (q < tot) {
+                    const uint32_t j  = (q >= p1) + (q >= p2) + (q >= p3);  // blocks with no chunks never match last
+                    const uint32_t pj = j == 0 ? 0u : j == 1 ? p1 : j == 2 ? p2 : p3;
+                    val[u]            = __ldcg(J.slots + (size_t)(b0 + j) * kChunks + (q - pj));
+                }
             }
-        }
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (qq[u] < tot) B[qq[u]] = v[u];
+            for (int u = 0; u < 4; ++u)
+                if (q0 + u * 32 < tot) B[q0 + u * 32] = val[u];
+        }
     }
     // the field's last item to finish: header, offset-table total, resets
-    __threadfence();  // this thread's stream writes before the count
     __syncthreads();
     if (tid == 0) *s_last = atomicAdd(&J.ctl->c_done, 1u) == J.nc - 1;
     __syncthreads();
     if (!*s_last) return;
-    __threadfence();
+    __threadfence();  // the other items' counts of c_done came before: the group sums are final
     const uint32_t nsup    = (uint32_t)cdiv(a.nb, kSuperBlocks);
     uint32_t       total_c = 0;
     for (uint32_t k = tid; k < nsup; k += blockDim.x) total_c += __ldcg(J.supers + k);
@@ -1211,12 +1362,29 @@ __global__ void __launch_bounds__(256) k_range_fields(const FieldJob* __restrict
     }
 }
 
+// Ring depth (group rows in flight per warp) of the encode kernels: 1D only.  Measured on
+// GB300 (encode launch, relative eb 1e-3): 1D 2^25 elements 49.2 -> 45.3 us with 4 rows at
+// 3 CTAs/SM; 2D exafel-like 27.1 -> 29.2 us and cesm-like 16.6 -> 17.4 us, so 2D keeps its
+// one row of register lookahead at 5 CTAs/SM (the extra warps hide more than the ring).
+template <int ND>
+__host__ __device__ constexpr int encode_ring() { return ND == 1 ? kEncodeRing : 0; }
+template <int ND>
+__host__ __device__ constexpr int encode_ctas() { return ND == 3 ? 4 : (ND == 1 && kEncodeRing ? kEncodeCtas : 5); }
+// Dynamic shared memory of an encode CTA: per warp the code image and the ring.
+template <int ND>
+__host__ __device__ constexpr uint32_t encode_smem() { return kCompressWarps * (kBlockWords * 4 + 1024u * encode_ring<ND>()); }
+
 template <int ND, bool kList>
-__global__ void __launch_bounds__(kCompressWarps * 32, ND == 3 ? 4 : 5)
+__global__ void __launch_bounds__(kCompressWarps * 32, encode_ctas<ND>())
     k_encode_fields(const FieldJob* __restrict__ jobs, const Segment* __restrict__ segs, uint32_t nseg, uint32_t total,
                     const __grid_constant__ FieldJob one)
 {
-    __shared__ __align__(16) uint32_t smem[kCompressWarps][kBlockWords];
+    // per warp: the block's 4 KiB code image, then (1D/2D) its ring of input rows
+    extern __shared__ __align__(16) uint32_t esm[];
+    constexpr int kR = encode_ring<ND>();
+    uint32_t*     smem = esm + (threadIdx.x >> 5) * kBlockWords;
+    float4*       ring = kR ? reinterpret_cast<float4*>(esm + kCompressWarps * kBlockWords) + (threadIdx.x >> 5) * kR * 64
+                            : nullptr;
     __shared__ float    s_r;
     __shared__ uint32_t s_rf;
     if (threadIdx.x == 0) s_rf = 0xFFFFFFFFu;
@@ -1231,7 +1399,7 @@ __global__ void __launch_bounds__(kCompressWarps * 32, ND == 3 ? 4 : 5)
             s_rf = f;
         }
         __syncthreads();
-        encode_item<ND>(J, i, s_r, smem[threadIdx.x >> 5]);
+        encode_item<ND, kR>(J, i, s_r, smem, ring);
         __syncthreads();  // the blocks' shared images before the next item
     }
 }
@@ -1240,11 +1408,11 @@ template <bool kList>
 __global__ void __launch_bounds__(256) k_compact_fields(const FieldJob* __restrict__ jobs, const Segment* __restrict__ segs,
                                                         uint32_t nseg, uint32_t total, const __grid_constant__ FieldJob one)
 {
-    __shared__ uint32_t s_red[2][kCompressWarps], s_pre[kCompactBlocks], s_tot, s_last;
+    __shared__ uint32_t s_red[kCompressWarps], s_last;
     for (uint32_t k = blockIdx.x; k < total; k += gridDim.x) {
         uint32_t f = 0, i = k;
         if (kList) locate(segs, nseg, k, f, i);
-        compact_item(kList ? jobs[f] : one, i, s_red[0], s_red[1], s_pre, &s_tot, &s_last);
+        compact_item(kList ? jobs[f] : one, i, s_red, &s_last);
         __syncthreads();
     }
 }
@@ -1274,7 +1442,9 @@ static uint32_t resident_ctas(K kernel, int threads, int dyn_smem = 0)
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    if (dyn_smem > 48 * 1024 &&
+    // the opt-in is needed once static + dynamic shared memory passes 48 KiB; made for any
+    // dynamic size (it only raises the kernel's limit)
+    if (dyn_smem > 0 &&
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem) != cudaSuccess)
         return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, dyn_smem) != cudaSuccess) return 0;
@@ -1306,17 +1476,18 @@ static uint32_t list_wave(int which, bool list)
     uint32_t               w    = slot ? slot->load(std::memory_order_acquire) : 0u;
     if (w) return w;
     constexpr int T = kCompressWarps * 32;
+    // resident_ctas also opts the encode kernels in to their dynamic shared memory
     if (list) {
         w = which == 0 ? resident_ctas(k_range_fields<true>, T)
-            : which == 1 ? resident_ctas(k_encode_fields<1, true>, T)
-            : which == 2 ? resident_ctas(k_encode_fields<2, true>, T)
-            : which == 3 ? resident_ctas(k_encode_fields<3, true>, T)
+            : which == 1 ? resident_ctas(k_encode_fields<1, true>, T, encode_smem<1>())
+            : which == 2 ? resident_ctas(k_encode_fields<2, true>, T, encode_smem<2>())
+            : which == 3 ? resident_ctas(k_encode_fields<3, true>, T, encode_smem<3>())
                          : resident_ctas(k_compact_fields<true>, T);
     } else {
         w = which == 0 ? resident_ctas(k_range_fields<false>, T)
-            : which == 1 ? resident_ctas(k_encode_fields<1, false>, T)
-            : which == 2 ? resident_ctas(k_encode_fields<2, false>, T)
-            : which == 3 ? resident_ctas(k_encode_fields<3, false>, T)
+            : which == 1 ? resident_ctas(k_encode_fields<1, false>, T, encode_smem<1>())
+            : which == 2 ? resident_ctas(k_encode_fields<2, false>, T, encode_smem<2>())
+            : which == 3 ? resident_ctas(k_encode_fields<3, false>, T, encode_smem<3>())
                          : resident_ctas(k_compact_fields<false>, T);
     }
     if (slot) slot->store(w, std::memory_order_release);
@@ -1341,15 +1512,15 @@ cudaError_t launch_fields(FieldPhase phase, int nd, const FieldJob* jobs, const 
         else k_compact_fields<false><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one);
     } else if (list) {
         switch (nd) {
-        case 1: k_encode_fields<1, true><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one); break;
-        case 2: k_encode_fields<2, true><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one); break;
-        default: k_encode_fields<3, true><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one); break;
+        case 1: k_encode_fields<1, true><<<grid, block, encode_smem<1>(), s>>>(jobs, segs, nseg, total, one); break;
+        case 2: k_encode_fields<2, true><<<grid, block, encode_smem<2>(), s>>>(jobs, segs, nseg, total, one); break;
+        default: k_encode_fields<3, true><<<grid, block, encode_smem<3>(), s>>>(jobs, segs, nseg, total, one); break;
         }
     } else {
         switch (nd) {
-        case 1: k_encode_fields<1, false><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one); break;
-        case 2: k_encode_fields<2, false><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one); break;
-        default: k_encode_fields<3, false><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one); break;
+        case 1: k_encode_fields<1, false><<<grid, block, encode_smem<1>(), s>>>(jobs, segs, nseg, total, one); break;
+        case 2: k_encode_fields<2, false><<<grid, block, encode_smem<2>(), s>>>(jobs, segs, nseg, total, one); break;
+        default: k_encode_fields<3, false><<<grid, block, encode_smem<3>(), s>>>(jobs, segs, nseg, total, one); break;
         }
     }
     return cudaGetLastError();
