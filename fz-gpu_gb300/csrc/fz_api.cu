@@ -223,7 +223,7 @@ fz_status fz_workspace_bytes(uint64_t max_n, uint64_t* bytes)
     b += 16;                        // range accumulators
     b += pad16(2 * max_n + 16);     // per-block slots (k_encode)
     b += pad16(4 * tiles + 4);      // block offsets
-    b += pad16(4 * (tiles / 512 + 2));  // chunk counts per 512 blocks
+    b += pad16(4 * (tiles / kSuperBlocks + 2));  // chunk counts per group of blocks
     *bytes = b;
     return FZ_SUCCESS;
 }
@@ -669,7 +669,7 @@ fz_status fz_decompress_batch(fz_workspace* ws, const fz_field* fields, uint32_t
 namespace {
 
 // Device work list of a batch compression, in one allocation: every field's job and
-// control words, its slots (4 KiB per shuffle block), block counts and 512-block group
+// control words, its slots (4 KiB per shuffle block), block counts and group
 // sums, and the segment tables of the range launch, of the encode launch of each
 // dimensionality and of the compaction launch.
 struct ListPlan {

@@ -7,7 +7,7 @@
 //                 compacted into its own slot (encodeDebug, fz.cu:49-59); independent
 //                 CTAs, one 2048-code shuffle block per warp.
 //   k_compact     the prefix sum over the blocks' chunk counts (replacing
-//                 cub::DeviceScan, fz.cu:187-201) from per-512-block sums, the move of
+//                 cub::DeviceScan, fz.cu:187-201) from per-group sums, the move of
 //                 the chunks to their final offsets, the offset table and the header.
 //   k_compress    the same forward path in a single launch with a decoupled look-back
 //                 over scan tiles (persistent, software pipelined); used where no
@@ -1133,7 +1133,7 @@ __global__ void __launch_bounds__(kCompressWarps * 32, 3) k_compress(const Compr
 //   k_encode_fields    encode items: 8 shuffle blocks, one per warp -- codes, bitshuffle,
 //                      chunk flags, bitmap words, sidecar, the block's non-zero chunks
 //                      compacted into its own 4 KiB slot, its count into counts[] and the
-//                      sum of its 512-block group; no CTA waits for another
+//                      sum of its group of 64 blocks; no CTA waits for another
 //   k_compact_fields   compaction items: 32 blocks -- every block's chunk offset (all
 //                      counts are known: the group sums before it plus the counts in its
 //                      group), the offset table, the chunks moved from the slots to
@@ -1265,7 +1265,7 @@ __device__ __forceinline__ void encode_item(const FieldJob& J, uint32_t i, float
 
 // Compaction item i of field J: blocks [32 i, 32 i + 32), four per warp, each warp on its
 // own (no CTA barrier until the item's end).  A warp's first chunk offset is the sum of
-// the group sums (512 blocks each) before its group plus the counts of the blocks of its
+// the group sums (kSuperBlocks blocks each) before its group plus the counts of the blocks of its
 // group before its own; then it writes the offset table entries of its 4 blocks and moves
 // their chunks from the slots to Section B (output chunk q of the warp comes from the last
 // of its blocks whose prefix is <= q; 16-byte loads, four in flight per lane).  The field's
@@ -1279,10 +1279,12 @@ __device__ __forceinline__ void compact_item(const FieldJob& J, uint32_t i, uint
     const CompressArgs& a   = J.a;
     const uint32_t      b0  = i * kCompactBlocks + wid * kCompactWarpBlocks, sup = b0 / kSuperBlocks;
     if (b0 < a.nb) {
+        static_assert(kSuperBlocks <= 64, "counts before a warp's blocks in its group: two per lane");
         uint32_t acc = 0;
         for (uint32_t k = lane; k < sup; k += 32) acc += __ldcg(J.supers + k);
-#pragma unroll 4
-        for (uint32_t b = sup * kSuperBlocks + lane; b < b0; b += 32) acc += __ldcg(J.counts + b);
+        const uint32_t g0 = sup * kSuperBlocks;
+        if (g0 + lane < b0) acc += __ldcg(J.counts + g0 + lane);
+        if (g0 + 32 + lane < b0) acc += __ldcg(J.counts + g0 + 32 + lane);
         const uint32_t c   = lane < kCompactWarpBlocks && b0 + lane < a.nb ? __ldcg(J.counts + b0 + lane) : 0u;
         const uint32_t exc = __reduce_add_sync(kFull, acc);
         // inclusive prefix of the 4 counts in lanes 0..3

@@ -75,7 +75,7 @@ struct FieldJob {
     FieldCtl*    ctl;
     uint4*       slots;   // 4 KiB per shuffle block
     uint32_t*    counts;  // chunks per block
-    uint32_t*    supers;  // chunks per 512 blocks (zero on entry, left zero)
+    uint32_t*    supers;  // chunks per group of kSuperBlocks blocks (zero on entry, left zero)
     uint32_t     nr, ne, nc;  // range, encode, compaction items
     uint32_t     rel;         // relative eb: the eb follows from the range items
 };
@@ -88,7 +88,9 @@ struct Segment {
 
 enum class FieldPhase { Range, Encode, Compact };
 
-constexpr uint32_t kSuperBlocks = 512;  // shuffle blocks per group sum of chunk counts
+// Shuffle blocks per group sum of chunk counts: a compaction warp's offset is the sum of
+// the group sums before its group plus at most 63 counts inside it -- one round of loads.
+constexpr uint32_t kSuperBlocks = 64;
 
 // Items of each kind for a field of n elements (ntiles scan tiles of shuffle blocks, nb full
 // blocks).

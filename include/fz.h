@@ -375,11 +375,15 @@ typedef struct fz_completion {
 /* A request loop with continuous batching under an HBM budget: `slots` streams, each with
    its own workspace, share one device pool of hbm_budget bytes from which every admitted
    host-buffer request takes its input and output buffers (a device-resident request
-   counts its input and output bytes against the same budget).  Requests queue in arrival order;
-   the server's worker threads (up to 8, each owning some slots) retire finished requests
-   and admit queued ones as slots and pool memory free up, so requests that arrive while
-   others run overlap on the device; fz_server_poll (non-blocking) hands out the
-   completions.  The functions may be called from any thread.  No counterpart in the
+   counts its input and output bytes against the same budget).  Requests queue in arrival
+   order; the server's worker threads (up to 8, each owning some slots) retire finished
+   requests and admit queued ones as slots and pool memory free up, so requests that arrive
+   while others run overlap on the device; fz_server_poll (non-blocking) hands out the
+   completions.  Admission looks at the first 64 queued requests: one may start ahead of
+   earlier ones that cannot (pool memory, or the cap of max(1, slots/4) host-buffer requests
+   with more than 32 MiB of copies running at once -- those keep their order among
+   themselves), and host copies go out in 8 MiB pieces so that small requests' copies are
+   not held behind a large one's.  The functions may be called from any thread.  No counterpart in the
    reference (one field per process, fz.cu:226-238). */
 typedef struct fz_server fz_server;
 fz_status fz_server_create(uint64_t hbm_budget, uint32_t slots, uint64_t max_n, fz_server** out);
