@@ -1,29 +1,33 @@
 #!/usr/bin/env python
 """Benchmark of the FZ compression hot path on GB300.
 
-A step is one pass of the path over one batch of synthetic input: `--fields` (8)
-independent exafel-like 39200x388 float32 fields (the single-field workload the metric
-is quoted on, relative eb 1e-3), each compressed (range pass, encode,
-compaction) and then decompressed (fused decode + inverse Lorenzo) on the device,
-issued as one CUDA-graph replay (fz_batch_create_pair: each field's compression and
-then its decompression on one of several parallel branches).  The
-batch holds 8 x 60.8 MB = 486 MB of input, larger than the 129 MB L2, and every field
-is visited once per step, so each step reads its inputs from HBM.
+A step is one pass of the path over one batch of synthetic input: `--fields` (128)
+exafel-like 39200x388 float32 fields (the single-field workload the metric is quoted on,
+relative eb 1e-3; `--distinct` seeded fields, each held in several device buffers), each
+compressed (range pass, encode, compaction) and then decompressed (fused decode + inverse
+Lorenzo), issued as one CUDA-graph replay of a round-trip batch under the schedule the
+autotuner picks.  A step holds 128 x 60.8 MB = 7.8 GB of input, far larger than the
+129 MB L2, and every buffer is visited once per step.
 
   value      uncompressed GB/s through the codec, both directions:
              steps * fields * 2 * 4n bytes / device time (CUDA events), summed over ranks
   e2e        the same metric through the host-buffer C-ABI calls fz_compress_host /
              fz_decompress_host (pinned host memory, H2D and D2H copies inside the region):
-             eight compressing host threads hand their streams to eight decompressing
-             ones, so input copies and output copies share the host link at all times
+             compressing host threads hand their streams to decompressing ones, so input
+             copies and output copies share the host link at all times
   roofline   the dominant kernel's algorithmic bytes per launch / its mean event-timed
              launch duration, against the measured HBM copy bandwidth
+  per_dimensionality  compress / decompress GB/s and kernel fractions of the other
+             single-field workloads (cesm-like 2D, hurricane-like 3D, unaligned rows, 1D)
+  batch      the 512-field mixed batch: every schedule the autotuner tries against the
+             plain per-field path
+  serving    a Poisson request trace over the same mix through the request loop
   cpu_baseline  the oracle (C, OpenMP) on this host's cores, round trips of one field
 
 `--impl reference` times the reference path's CPU restatement (the oracle port; the
 reference has no CPU implementation and its GPU code is not a CPU baseline) on the
-same metric and workload.  Under torchrun each rank runs its own batch (weak scaling);
-only rank 0 prints.
+same metric and workload, with the same `config`.  Under torchrun each rank runs its own
+batch (weak scaling); only rank 0 prints.
 """
 from __future__ import annotations
 
@@ -54,21 +58,30 @@ METRIC = "compress/decompress GB/s + %HBM peak"
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
-    p.add_argument("--fields", type=int, default=8)
+    p.add_argument("--fields", type=int, default=128, help="field buffers per step")
+    p.add_argument("--distinct", type=int, default=8, help="distinct seeded fields among them")
     p.add_argument("--impl", choices=["fz", "reference"], default="fz")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--quick", action="store_true", help="headline only: no per-dimensionality, batch or serving keys")
     p.add_argument("--workload", choices=["exafel", "batch", "serving"], default="exafel",
                    help="exafel: the headline line (single-field workload, see --field); batch: 512 mixed "
                         "1D/2D/3D fields batched vs per field; serving: a Poisson request trace")
     p.add_argument("--field", choices=sorted(FIELDS), default="exafel",
                    help="the single-field workload of the headline line (default exafel)")
     p.add_argument("--batch-fields", type=int, default=512)
-    p.add_argument("--serve-seconds", type=float, default=3.0)
+    p.add_argument("--serve-seconds", type=float, default=2.0)
     p.add_argument("--serve-rate", type=float, default=2000.0)
+    p.add_argument("--serve-host-fields", type=int, default=128,
+                   help="fields of the mix (the first ones) that the host-buffer trace draws from")
     return p.parse_args()
+
+
+def config_dict(n):
+    """The `config` both arms print: the workload the metric is quoted on."""
+    return {"workload": WORKLOAD, "field_elems": n, "eb": EB, "eb_mode": "relative", "stream_mode": "sidecar"}
 
 
 def dist_env():
@@ -221,8 +234,8 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * el / args.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
-        "config": {"workload": WORKLOAD + ", one field per step (compress + decompress)",
-                   "field_elems": n},
+        "config": config_dict(n),
+        "run": {"step": "one round trip (compress + decompress) of one field on the host cores"},
         "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": oracle.threads(), "kind": "port",
                          "sample": f"{args.steps} round trips of one {'x'.join(map(str, DIMS))} field"},
         "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -243,21 +256,24 @@ def run_fz(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     L = fz.lib()
-    fields = make_fields(args.fields, rank_seed0(rank, args.fields))
+    nd_ = min(args.distinct, args.fields)
+    fields = make_fields(nd_, rank_seed0(rank, nd_))
     n = fields[0].size
+    nf = args.fields
     cap = fz.max_compressed_bytes(n, DIMS, fz.MODE_SIDECAR)
-    X = [torch.from_numpy(f).to(dev) for f in fields]
-    S = [torch.empty(cap, dtype=torch.uint8, device=dev) for _ in fields]
-    Y = [torch.empty(n, dtype=torch.float32, device=dev) for _ in fields]
+    # field buffer i holds distinct field i % distinct: every buffer is its own memory
+    X = [torch.from_numpy(fields[i % nd_]).to(dev) for i in range(nf)]
+    S = [torch.empty(cap, dtype=torch.uint8, device=dev) for _ in range(nf)]
+    Y = [torch.empty(n, dtype=torch.float32, device=dev) for _ in range(nf)]
     ws = fz.Workspace(n)
     stream = torch.cuda.current_stream(dev)
     sh = C.c_void_p(stream.cuda_stream)
     dims = fz._dims(DIMS)
 
-    # first pass: validate and keep each field's header (decompression takes it from
-    # the host, as a caller that just compressed would)
+    # first pass: validate and keep each field's header (decompression takes it from the
+    # host, as a caller that just compressed would)
     headers, sizes = [], []
-    for i in range(args.fields):
+    for i in range(nf):
         nb = C.c_uint64()
         fz._check("compress", L.fz_compress(ws.handle, C.c_void_p(X[i].data_ptr()), n, dims, EB, fz.EB_REL,
                                             fz.MODE_SIDECAR, C.c_void_p(S[i].data_ptr()), cap, C.byref(nb), sh))
@@ -265,10 +281,9 @@ def run_fz(args, rank, world, local_rank):
         headers.append(h)
         sizes.append(nb.value)
     comp = fz.fields_array([{"src": X[i].data_ptr(), "dst": S[i].data_ptr(), "n": n, "dims": DIMS, "eb": EB,
-                             "dst_capacity": cap} for i in range(args.fields)])
+                             "dst_capacity": cap} for i in range(nf)])
     dec = fz.fields_array([{"src": S[i].data_ptr(), "dst": Y[i].data_ptr(), "src_bytes": sizes[i],
-                            "dst_capacity": n, "header": headers[i]} for i in range(args.fields)])
-    nf = args.fields
+                            "dst_capacity": n, "header": headers[i]} for i in range(nf)])
 
     def step():
         # one ABI call per direction: the batch's kernels go out back to back
@@ -280,30 +295,12 @@ def run_fz(args, rank, world, local_rank):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    # spot check: the reconstruction of the last field meets the error bound
-    err = (Y[-1] - X[-1]).abs().max().item()
-    assert err <= headers[-1].eb_abs * (1 + 2 ** -10) + 1e-6 * X[-1].abs().max().item(), err
+    check_recon(X, Y, headers)
 
-    # Timed region 1 (value): the step replayed from one CUDA graph (fz_batch_create_pair:
-    # field i compressed then decompressed on one of `branches` parallel branches, so one
-    # field's decompression overlaps the others' compression).  The branch count is the
-    # fastest of a few, timed on these fields before the region.
-    def pair_ms(b, reps=3):
-        g_ = fz.Batch.pair(ws, comp, dec, branches=b)
-        for _ in range(2):
-            g_.launch(stream)
-        e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0_.record(stream)
-        for _ in range(reps):
-            g_.launch(stream)
-        e1_.record(stream)
-        torch.cuda.synchronize()
-        g_.close()
-        return e0_.elapsed_time(e1_) / reps
-
-    tuned = {b: pair_ms(b) for b in (4, 8, 16) if b <= 2 * nf}
-    bp = min(tuned, key=tuned.get)
-    gp = fz.Batch.pair(ws, comp, dec, branches=bp)
+    # Timed region 1 (value): the step replayed from one CUDA graph of the round-trip batch,
+    # under the schedule fz_batch_autotune_sched picks on these fields before the region.
+    best, tuned = fz.batch_autotune_schedule(ws, comp, dec, reps=2, stream=stream)
+    gp = fz.Batch.scheduled(ws, comp, dec, best)
     for _ in range(args.warmup):
         gp.launch(stream)
     torch.cuda.synchronize()
@@ -322,53 +319,30 @@ def run_fz(args, rank, world, local_rank):
             dist.barrier()
     ms = max_over_ranks(ev0.elapsed_time(ev1), dist, dev)
     gp.close()
-    err = (Y[-1] - X[-1]).abs().max().item()
-    assert err <= headers[-1].eb_abs * (1 + 2 ** -10) + 1e-6 * X[-1].abs().max().item(), err
+    check_recon(X, Y, headers)
 
-    # Timed region 2 (kernel durations): the same steps issued as one batch call per
-    # direction without graphs, every kernel launch bracketed by a pair of CUDA events on
-    # the launching stream (workspace timing).
-    ws.enable_timing(args.steps * args.fields * 5 + 16)
+    # Timed region 2 (kernel durations): steps issued as one batch call per direction
+    # without graphs, every kernel launch bracketed by a pair of CUDA events on the
+    # launching stream (workspace timing).
+    ksteps = max(1, min(args.steps, 2))
+    ws.enable_timing(ksteps * nf * 5 + 16)
     torch.cuda.synchronize()
     s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(ksteps):
         step()
     s1.record(stream)
     torch.cuda.synchronize()
     calls_ms = s0.elapsed_time(s1)
-    kern = {}
-    for k in fz.Workspace.KERNELS:
-        if k != "-":
-            kern[k] = ws.kernel_time(k)
+    kern = {k: ws.kernel_time(k) for k in fz.Workspace.KERNELS}
     ws.enable_timing(0)
-    launches = sum(c for c, _ in kern.values())  # per timed region (both regions launch the same)
+    launches = args.steps * sum(c for c, _ in kern.values()) // ksteps  # region 1 launches the same kernels
 
-    bytes_step = args.fields * 2 * 4 * n
+    bytes_step = nf * 2 * 4 * n
     value = bytes_step * args.steps * world / (ms / 1e3) / 1e9
     hbm, src = peaks()
     stream_b = float(np.mean(sizes))
-    nb = n // 2048
-    # algorithmic bytes per launch: k_range_fields 4n read; k_encode_fields (codes,
-    # bitshuffle, flags, per-block compaction into slots) 4n read + the chunks written;
-    # k_compact_fields the chunks moved from the slots to Section B (read + write) + the
-    # counts and offsets; k_decompress (decode fused with the inverse Lorenzo) the stream
-    # read + 4n written
-    algo = {"k_range_fields": 4 * n, "k_encode_fields": 4 * n + stream_b,
-            "k_compact_fields": 2 * stream_b + 8 * (nb + 1), "k_offsets": 4 * ((n + 255) // 256) + 4 * (nb + 1),
-            "k_decompress": stream_b + 4 * n, "k_recon": 2 * n + 4 * n}
-    nd = 3 if DIMS[2] > 1 else (2 if DIMS[1] > 1 else 1)
-    # the names ncu shows: the encode kernel is templated on the dimensionality, the fused
-    # decompression kernel has one variant per dimensionality
-    shown = {"k_encode_fields": f"k_encode_fields<{nd}>", "k_decompress": f"k_decompress{nd}d"}
-    kernels = {}
-    for k, (cnt, tot) in kern.items():
-        if cnt:
-            us = 1e3 * tot / cnt
-            gbs = algo[k] / (us * 1e-6) / 1e9
-            kernels[shown.get(k, k)] = {"launches": cnt, "mean_us": round(us, 3), "algo_bytes": int(algo[k]),
-                                        "achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm, 4),
-                                        "share": round(tot / sum(v[1] for v in kern.values()), 4)}
+    kernels, t_c, t_d = kernel_table(kern, n, stream_b, DIMS, hbm)
     dom = max(kernels, key=lambda k: kernels[k]["launches"] * kernels[k]["mean_us"])
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
@@ -377,20 +351,21 @@ def run_fz(args, rank, world, local_rank):
             traffic = json.load(open(tpath)).get(dom, {}).get("dram_bytes_per_launch")
         except Exception:
             traffic = None
-    t_c = sum(kern[k][1] for k in ("k_range_fields", "k_encode_fields", "k_compact_fields")) / max(
-        1, kern["k_encode_fields"][0])
-    t_d = sum(kern[k][1] for k in ("k_offsets", "k_decompress", "k_recon")) / max(1, kern["k_decompress"][0])
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator standing in for the EXAFEL field, no dataset)",
-        "config": {"workload": WORKLOAD, "fields_per_step": args.fields, "field_elems": n,
-                   "schedule": f"one graph per step, field i compress -> decompress on branch i % {bp}",
-                   "mode": "sidecar", "stream_bytes_mean": int(stream_b),
-                   "ratio_reference_formula": round(fz.reference_sizes(4 * n, headers[0].nnz)[2], 4),
-                   "l2": f"inputs {args.fields * 4 * n / 1e6:.0f} MB per step > 129 MB L2; each field visited once per step"},
-        "value_without_graphs": round(bytes_step * args.steps * world / (calls_ms / 1e3) / 1e9, 2),
+        "config": config_dict(n),
+        "run": {"fields_per_step": nf, "distinct_fields": nd_,
+                "schedule": {"branches": best.branches, "list": best.list,
+                             "tuned_ms": {f"{'list+' if l else ''}{b} branches": round(t, 3)
+                                          for (b, l), t in tuned.items()}},
+                "stream_bytes_mean": int(stream_b),
+                "ratio_reference_formula": round(fz.reference_sizes(4 * n, headers[0].nnz)[2], 4),
+                "timed_region_ms": round(ms, 2),
+                "l2": f"inputs {nf * 4 * n / 1e9:.1f} GB per step > 129 MB L2; each buffer visited once per step"},
+        "value_without_graphs": round(bytes_step * ksteps * world / (calls_ms / 1e3) / 1e9, 2),
         "compress_gbs": round(4 * n / (t_c * 1e-3) / 1e9, 1),
         "decompress_gbs": round(4 * n / (t_d * 1e-3) / 1e9, 1),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": kernels[dom]["achieved_gbs"], "peak": hbm,
@@ -402,6 +377,14 @@ def run_fz(args, rank, world, local_rank):
     }
     if not args.no_e2e:
         line["e2e"] = e2e(fz, L, fields, n, cap, sizes, args, dev, world, dist)
+    del X, S, Y
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and not args.quick:
+        line["per_dimensionality"] = per_dimensionality(fz, dev, hbm)
+        torch.cuda.empty_cache()
+        line["batch"] = run_batch(args, local_rank)
+        torch.cuda.empty_cache()
+        line["serving"] = run_serving(args, local_rank)
     if rank == 0 and world == 1:
         import oracle
         oracle.build()
@@ -418,6 +401,109 @@ def run_fz(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def check_recon(X, Y, headers):
+    """Spot check: the reconstructions of the first and last buffers meet the error bound."""
+    for i in (0, len(X) - 1):
+        err = (Y[i] - X[i]).abs().max().item()
+        assert err <= headers[i].eb_abs * (1 + 2 ** -10) + 1e-6 * X[i].abs().max().item(), err
+
+
+def kernel_table(kern, n, stream_b, dims, hbm):
+    """Per kernel (by the name ncu shows): launches, mean event-timed duration, algorithmic
+    bytes per launch, achieved GB/s and fraction of the HBM peak, share of kernel time;
+    plus the compression and decompression time per field (ms)."""
+    nb = n // 2048
+    # algorithmic bytes per launch: k_range_fields 4n read; k_encode_fields (codes,
+    # bitshuffle, flags, per-block compaction into slots) 4n read + the chunks written;
+    # k_compact_fields the chunks moved from the slots to Section B (read + write) + the
+    # counts and offsets; k_decompress (decode fused with the inverse Lorenzo) the stream
+    # read + 4n written
+    algo = {"k_range_fields": 4 * n, "k_encode_fields": 4 * n + stream_b,
+            "k_compact_fields": 2 * stream_b + 8 * (nb + 1), "k_offsets": 4 * ((n + 255) // 256) + 4 * (nb + 1),
+            "k_decompress": stream_b + 4 * n, "k_recon": 2 * n + 4 * n}
+    nd = 3 if dims[2] > 1 else (2 if dims[1] > 1 else 1)
+    # the names ncu shows: the encode kernel is templated on the dimensionality, the fused
+    # decompression kernel has one variant per dimensionality
+    shown = {"k_encode_fields": f"k_encode_fields<{nd}>", "k_decompress": f"k_decompress{nd}d"}
+    total = sum(v[1] for v in kern.values()) or 1.0
+    kernels = {}
+    for k, (cnt, tot) in kern.items():
+        if cnt:
+            us = 1e3 * tot / cnt
+            gbs = algo[k] / (us * 1e-6) / 1e9
+            kernels[shown.get(k, k)] = {"launches": cnt, "mean_us": round(us, 3), "algo_bytes": int(algo[k]),
+                                        "achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm, 4),
+                                        "share": round(tot / total, 4)}
+    per = max(1, kern["k_encode_fields"][0])
+    t_c = sum(kern[k][1] for k in ("k_range_fields", "k_encode_fields", "k_compact_fields")) / per
+    t_d = sum(kern[k][1] for k in ("k_offsets", "k_decompress", "k_recon")) / max(1, kern["k_decompress"][0])
+    return kernels, t_c, t_d
+
+
+# single-field workloads of the other dimensionalities and row widths: (name, kind, dims,
+# relative eb, device buffers per step); every step's input exceeds the L2
+OTHERS = [("cesm-like 3600x1800", "smooth2d", (3600, 1800, 1), 1e-3, 16),
+          ("hurricane-like 500x500x100", "smooth3d", (500, 500, 100), 1e-3, 6),
+          ("hurricane-like 500x500x100 eb 1e-2", "smooth3d", (500, 500, 100), 1e-2, 6),
+          ("exafel-like 39201x388 (rows not a multiple of 4)", "peaks2d", (39201, 388, 1), 1e-3, 8),
+          ("1D 2^25", "smooth1d", (1 << 25, 1, 1), 1e-3, 4)]
+
+
+def per_dimensionality(fz, dev, hbm):
+    """For each workload of OTHERS: compress-only and decompress-only batch graphs over its
+    buffers (8 branches), replayed (GB/s of uncompressed bytes per direction), and the
+    kernels' event times from a pass of plain calls."""
+    import importlib
+    import torch
+    synth = importlib.import_module("fz_gpu_gb300.synth")
+    out = {}
+    for name, kind, dims, eb, copies in OTHERS:
+        f = synth.field(kind, dims, 7)
+        n = f.size
+        x0 = torch.from_numpy(f).to(dev)
+        X = [x0.clone() for _ in range(copies)]
+        del x0
+        cap = fz.max_compressed_bytes(n, dims)
+        S = [torch.empty(cap, dtype=torch.uint8, device=dev) for _ in range(copies)]
+        Y = [torch.empty(n, dtype=torch.float32, device=dev) for _ in range(copies)]
+        ws = fz.Workspace(n)
+        heads, sizes = [], []
+        for i in range(copies):
+            st = fz.compress(X[i], dims, eb, ws=ws, out=S[i])
+            heads.append(fz.parse_header(st[:64].cpu().numpy()))
+            sizes.append(st.numel())
+        comp = fz.fields_array([{"src": X[i].data_ptr(), "dst": S[i].data_ptr(), "n": n, "dims": dims, "eb": eb,
+                                 "dst_capacity": cap} for i in range(copies)])
+        dec = fz.fields_array([{"src": S[i].data_ptr(), "dst": Y[i].data_ptr(), "src_bytes": sizes[i],
+                                "dst_capacity": n, "header": heads[i]} for i in range(copies)])
+        res = {"field_elems": n, "buffers": copies, "ratio_reference_formula":
+               round(fz.reference_sizes(4 * n, heads[0].nnz)[2], 3)}
+        for what, g in (("compress", fz.Batch.scheduled(ws, comp, None, fz.Schedule(8, 0))),
+                        ("decompress", fz.Batch.scheduled(ws, None, dec, fz.Schedule(8, 0)))):
+            for _ in range(3):
+                g.launch()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(5):
+                g.launch()
+            e1.record()
+            torch.cuda.synchronize()
+            res[what + "_gbs"] = round(copies * 4 * n * 5 / (e0.elapsed_time(e1) * 1e-3) / 1e9, 1)
+            g.close()
+        ws.enable_timing(copies * 5 + 8)
+        for i in range(copies):
+            fz.compress(X[i], dims, eb, ws=ws, out=S[i], readback=False)
+            fz.decompress(S[i], header=heads[i], ws=ws, out=Y[i])
+        torch.cuda.synchronize()
+        kern = {k: ws.kernel_time(k) for k in fz.Workspace.KERNELS}
+        kt, _, _ = kernel_table(kern, n, float(sum(sizes)) / copies, dims, hbm)
+        res["kernels"] = {k: {"mean_us": v["mean_us"], "frac": v["frac"]} for k, v in kt.items()}
+        out[name] = res
+        del X, S, Y, ws
+        torch.cuda.empty_cache()
+    return out
 
 
 # host threads on each side of the e2e pipeline: compressing threads hand their streams
@@ -438,8 +524,9 @@ def e2e(fz, L, fields, n, cap, sizes, args, dev, world, dist):
     import queue
     import numpy as np
     import torch
-    steps = min(args.steps, 30)
-    nf = len(fields)
+    steps = min(args.steps, 5)
+    nf = args.fields  # round trips per step, as in the device-timed step (field i % distinct)
+    nd_ = len(fields)
     items = steps * nf
     T = E2E_THREADS
     hin = [torch.from_numpy(f).pin_memory() for f in fields]
@@ -472,9 +559,9 @@ def e2e(fz, L, fields, n, cap, sizes, args, dev, world, dist):
         try:
             for j in range(k, items, T):
                 buf = free.get(timeout=120)  # raises if the decompressing side has stopped
-                nb = compress(w, j % nf, buf)
+                nb = compress(w, (j % nf) % nd_, buf)
                 w["bytes"] += nb
-                ready.put((buf, nb, j % nf))
+                ready.put((buf, nb, (j % nf) % nd_))
         except Exception as ex:  # surfaced after join
             w["err"] = ex
             ready.put(None)
@@ -541,9 +628,12 @@ def _torch_fields(specs, dev):
 
 
 def run_batch(args, local_rank):
-    """A mixed batch of 512 fields (log-uniform 64 KB-256 MB, 1D/2D/3D, eb from
-    {1e-2,1e-3,1e-4}) compressed and decompressed from two CUDA-graph replays, against the
-    plain per-field path (fz_compress with its size readback, then fz_decompress)."""
+    """The 512-field mixed batch (log-uniform 64 KB-256 MB, 1D/2D/3D, eb from
+    {1e-2,1e-3,1e-4}) compressed and decompressed as one round-trip CUDA-graph replay under
+    every schedule fz_batch_autotune_sched tries (per-field launches on 1-16 parallel
+    branches, or the compression as list launches over a device work list of all fields),
+    against the plain per-field path (fz_compress with its size readback, then
+    fz_decompress, one field at a time).  Returns the figures as a dict."""
     import importlib
     import torch
     import __graft_entry__ as g
@@ -560,7 +650,7 @@ def run_batch(args, local_rank):
     ws = fz.Workspace(max(ns))
     total = 4 * sum(ns)
     stream = torch.cuda.current_stream(dev)
-    # plain per-field path, as a caller handling one field at a time
+
     def plain():
         for x, s_, y, (_, d, eb, _) in zip(X, S, Y, specs):
             st = fz.compress(x, d, eb, ws=ws, out=s_)
@@ -573,49 +663,52 @@ def run_batch(args, local_rank):
     t_plain = time.perf_counter() - t0
     heads = [fz.parse_header(s_[:64].cpu().numpy()) for s_ in S]
     sizes = [fz.stream_bytes(h) for h in heads]
+    ref = [s_[:b].clone() for s_, b in zip(S[:16], sizes[:16])]
     comp = fz.fields_array([{"src": x.data_ptr(), "dst": s_.data_ptr(), "n": n, "dims": d, "eb": eb,
                              "dst_capacity": s_.numel()} for x, s_, n, (_, d, eb, _) in zip(X, S, ns, specs)])
     dec = fz.fields_array([{"src": s_.data_ptr(), "dst": y.data_ptr(), "src_bytes": b, "dst_capacity": y.numel(),
                             "header": h} for s_, y, b, h in zip(S, Y, sizes, heads)])
-    # autotuner: branch count per direction, timed on these fields (fz_batch_autotune)
-    bc, msc = fz.batch_autotune(ws, comp, fz.COMPRESS, reps=2, stream=stream)
-    bd, msd = fz.batch_autotune(ws, dec, fz.DECOMPRESS, reps=2, stream=stream)
-    gc, gd = fz.Batch(ws, comp, fz.COMPRESS, branches=bc), fz.Batch(ws, dec, fz.DECOMPRESS, branches=bd)
+    best, tuned = fz.batch_autotune_schedule(ws, comp, dec, reps=2, stream=stream)
+    gb = fz.Batch.scheduled(ws, comp, dec, best)
     for _ in range(2):
-        gc.launch(stream), gd.launch(stream)
+        gb.launch(stream)
     torch.cuda.synchronize()
     steps = max(1, min(args.steps, 5))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(steps):
-        gc.launch(stream), gd.launch(stream)
+        gb.launch(stream)
     e1.record(stream)
     torch.cuda.synchronize()
     t_batch = e0.elapsed_time(e1) / 1e3 / steps
-    # every stream of the replays equals the plain path's (which tests check bit for bit)
-    assert all(fz.parse_header(s_[:64].cpu().numpy()).nnz == h.nnz for s_, h in zip(S[:8], heads[:8]))
+    gb.close()
+    # the replays wrote the plain path's streams (which tests check bit for bit)
+    assert all(torch.equal(s_[: r.numel()], r) for s_, r in zip(S, ref))
     ratio = sum(4 * n for n in ns) / sum(sizes)
-    line = {"metric": "512 mixed fields: batched vs per-field aggregate GB/s (compress + decompress)",
-            "value": round(2 * total / t_batch / 1e9, 2), "unit": "GB/s",
-            "per_field_plain": round(2 * total / t_plain / 1e9, 2),
-            "speedup_vs_per_field": round(t_plain / t_batch, 2),
-            "fields": len(specs), "total_gb": round(total / 1e9, 3), "steps": steps,
-            "aggregate_ratio": round(ratio, 3), "higher_is_better": True,
-            "autotune": {"compress": {"branches": bc, "ms": {str(k): round(v, 3) for k, v in msc.items()}},
-                         "decompress": {"branches": bd, "ms": {str(k): round(v, 3) for k, v in msd.items()}}},
-            "data": "synthetic (seeded device-side generators)",
-            "config": {"workload": "mixed 1D/2D/3D, sizes log-uniform 64 KB-256 MB, eb in {1e-2,1e-3,1e-4}",
-                       "batched": "two CUDA-graph replays (fz_batch_launch), branch counts from fz_batch_autotune",
-                       "per_field": "fz_compress with size readback + fz_decompress, one field at a time"}}
-    print(json.dumps(line), flush=True)
+    gbs = lambda t: round(2 * total / t / 1e9, 2)
+    out = {"metric": "512 mixed fields: batched vs per-field aggregate GB/s (compress + decompress)",
+           "value": gbs(t_batch), "unit": "GB/s", "per_field_plain": gbs(t_plain),
+           "speedup_vs_per_field": round(t_plain / t_batch, 2),
+           "schedule": {"branches": best.branches, "list": best.list},
+           "schedules_gbs": {f"{'list+' if l else ''}{b} branches": gbs(t / 1e3) for (b, l), t in tuned.items()},
+           "fields": len(specs), "total_gb": round(total / 1e9, 3), "steps": steps,
+           "aggregate_ratio": round(ratio, 3), "higher_is_better": True,
+           "data": "synthetic (seeded device-side generators)",
+           "config": {"workload": "mixed 1D/2D/3D, sizes log-uniform 64 KB-256 MB, eb in {1e-2,1e-3,1e-4}",
+                      "batched": "one round-trip CUDA-graph replay (fz_batch_launch) per step, schedule from "
+                                 "fz_batch_autotune_sched",
+                      "per_field": "fz_compress with size readback + fz_decompress, one field at a time"}}
+    del X, S, Y, ref
+    return out
 
 
 def run_serving(args, local_rank):
-    """Poisson arrivals (mean --serve-rate req/s) of fields drawn as in the mixed batch,
-    60/40 compress/decompress, served by the request loop (8 slots, HBM
-    budget) against the same trace served one request at a time (1 slot).  Two request
-    kinds: device-resident fields (FZ_REQUEST_DEVICE, the fields and results live in HBM)
-    and host buffers (pinned; H2D/D2H copies per request)."""
+    """Poisson arrivals (mean --serve-rate req/s) of fields drawn from the 512-field mix,
+    60/40 compress/decompress, served by the request loop (8 slots, HBM budget) against
+    the same trace served one request at a time (1 slot).  Two request kinds:
+    device-resident fields (FZ_REQUEST_DEVICE, the fields and results live in HBM; drawn
+    from all 512 fields) and host buffers (pinned; H2D/D2H copies per request; drawn from
+    the first --serve-host-fields fields).  Returns the figures as a dict."""
     import importlib
     import numpy as np
     import torch
@@ -624,7 +717,7 @@ def run_serving(args, local_rank):
     synth = importlib.import_module("fz_gpu_gb300.synth")
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    specs = synth.mixed_specs(48, seed=4)
+    specs = synth.mixed_specs(args.batch_fields, seed=3)
     Xd = _torch_fields(specs, dev)
     ns = [x.numel() for x in Xd]
     ws = fz.Workspace(max(ns))
@@ -634,20 +727,23 @@ def run_serving(args, local_rank):
     heads = [fz.parse_header(s_[:64].cpu().numpy()) for s_ in Sd]
     out_c = [torch.empty(c, dtype=torch.uint8, device=dev) for c in caps]
     out_d = [torch.empty(n, dtype=torch.float32, device=dev) for n in ns]
-    hin = [x.cpu().pin_memory() for x in Xd]
-    hst = [s_.cpu().pin_memory() for s_ in Sd]
-    hout_c = [torch.empty(c, dtype=torch.uint8).pin_memory() for c in caps]
-    hout_d = [torch.empty(n, dtype=torch.float32).pin_memory() for n in ns]
+    nh = min(args.serve_host_fields, len(specs))
+    hin = [x.cpu().pin_memory() for x in Xd[:nh]]
+    hst = [s_.cpu().pin_memory() for s_ in Sd[:nh]]
+    hout_c = [torch.empty(c, dtype=torch.uint8).pin_memory() for c in caps[:nh]]
+    hout_d = [torch.empty(n, dtype=torch.float32).pin_memory() for n in ns[:nh]]
     torch.cuda.synchronize()
     rng = np.random.default_rng(4)
     nreq = int(args.serve_rate * args.serve_seconds)
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, nreq))
-    fields = rng.integers(0, len(specs), nreq)
+    draw = rng.random(nreq)
     comp = rng.random(nreq) < 0.6
     free = torch.cuda.mem_get_info(dev)[0]
     budget = int(min(120 << 30, free - (16 << 30)))
 
     def serve(slots, device, trace=True):
+        nf = len(specs) if device else nh
+        fields = (draw * nf).astype(np.int64)
         server = fz.Server(budget, slots, max(ns))
         lat = np.zeros(nreq)
 
@@ -703,6 +799,7 @@ def run_serving(args, local_rank):
     def plain():
         """The plain per-field path on the same trace, device-resident: fz_compress with
         its size readback, fz_decompress, one request at a time."""
+        fields = (draw * len(specs)).astype(np.int64)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for i in range(nreq):
@@ -720,14 +817,15 @@ def run_serving(args, local_rank):
     plain_gbs = plain()
     dev_mode["saturated_gbs"]["plain_per_field"] = round(plain_gbs, 2)
     dev_mode["saturated_gbs"]["speedup_vs_plain"] = round(dev_mode["saturated_gbs"]["slots8"] / plain_gbs, 2)
-    line = {"metric": "Poisson request trace: served latency and aggregate GB/s (uncompressed bytes)",
-            "requests": nreq, "rate_req_s": args.serve_rate, "hbm_budget_gb": round(budget / 2 ** 30, 1),
-            **dev_mode, "host_buffers": mode(False),
-            "data": "synthetic (seeded device-side generators, 48 distinct fields)",
-            "config": {"workload": "Poisson arrivals, 60/40 compress/decompress, fields as in the mixed batch",
-                       "requests": "device-resident fields and results (FZ_REQUEST_DEVICE); "
-                                   "host_buffers: the same trace with pinned host buffers"}}
-    print(json.dumps(line), flush=True)
+    out = {"metric": "Poisson request trace: served latency and aggregate GB/s (uncompressed bytes)",
+           "requests": nreq, "rate_req_s": args.serve_rate, "hbm_budget_gb": round(budget / 2 ** 30, 1),
+           "device_resident": dev_mode, "host_buffers": mode(False),
+           "data": f"synthetic (seeded device-side generators; {len(specs)}-field mix, host buffers: its first {nh})",
+           "config": {"workload": "Poisson arrivals, 60/40 compress/decompress, fields drawn from the 512-field mix",
+                      "requests": "device-resident fields and results (FZ_REQUEST_DEVICE); "
+                                  "host_buffers: the same kind of trace with pinned host buffers"}}
+    del Xd, Sd, out_c, out_d, hin, hst, hout_c, hout_d
+    return out
 
 
 def main():
@@ -739,10 +837,10 @@ def main():
         run_reference(args, rank, world)
     elif args.workload == "batch":
         if rank == 0:
-            run_batch(args, local_rank)
+            print(json.dumps(run_batch(args, local_rank)), flush=True)
     elif args.workload == "serving":
         if rank == 0:
-            run_serving(args, local_rank)
+            print(json.dumps(run_serving(args, local_rank)), flush=True)
     else:
         run_fz(args, rank, world, local_rank)
 
