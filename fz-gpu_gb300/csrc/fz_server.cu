@@ -7,7 +7,7 @@
 //   * `slots` execution slots, each a CUDA stream with its own workspace (scan state),
 //     a pinned 128-byte readback buffer and an event.
 // Requests wait in a queue (admission: see admit()).  Host-buffer requests (pinned ones let
-// the copies overlap) are staged through pool buffers, their copies issued in 8 MiB pieces; device-resident requests (FZ_REQUEST_DEVICE) run on
+// the copies overlap) are staged through pool buffers; device-resident requests (FZ_REQUEST_DEVICE) run on
 // the caller's device buffers and only count their bytes against the pool.
 // Worker threads (up to kWorkers, each owning every kWorkers-th slot) retire requests
 // whose work has finished and admit queued requests while a slot is free and the pool
@@ -84,7 +84,6 @@ private:
 enum class Phase { Idle, WaitInHeader, WaitHeader, WaitDone };
 
 struct Slot {
-    bool          large  = false;  // counts against the server's large-request limit
     cudaStream_t  stream = nullptr;
     fz_workspace* ws     = nullptr;
     uint8_t*      h_buf  = nullptr;  // pinned: header (64 B) + status word
@@ -104,27 +103,12 @@ uint64_t max_stream_bytes(uint64_t n, fz_dims d, fz_mode m)
     return fz_max_compressed_bytes(n, d, m, &b) == FZ_SUCCESS ? b : 0;
 }
 
-// Host<->device copies of a request go out in pieces of at most kCopyPiece bytes, so the
-// copy engines can interleave other slots' copies between them: a small request's copy
-// does not wait behind the whole of a 256 MB one.
-constexpr uint64_t kCopyPiece = 8ull << 20;
-
-cudaError_t copy_pieces(void* dst, const void* src, uint64_t bytes, cudaMemcpyKind kind, cudaStream_t s)
-{
-    for (uint64_t off = 0; off < bytes; off += kCopyPiece) {
-        const cudaError_t e = cudaMemcpyAsync(static_cast<uint8_t*>(dst) + off, static_cast<const uint8_t*>(src) + off,
-                                              std::min(kCopyPiece, bytes - off), kind, s);
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
-}
-
-// Admission.  A host-buffer request whose copies exceed kLargeBytes is "large": at most
-// max(1, slots / 4) of them run at once, so the host link is not split many ways (which
-// stretches every large request and the small ones queued behind them).  A request may
-// pass queued ones that cannot start (no memory yet, or the large ones' limit reached)
-// within the first kAdmitWindow queue entries; large ones among themselves stay in order.
-constexpr uint64_t kLargeBytes  = 32ull << 20;
+// Admission: a request may start ahead of earlier queued ones that are waiting for pool
+// memory, within the first kAdmitWindow queue entries (so a small request is not held
+// behind a large one that does not fit yet).  Measured on the host-buffer trace of the
+// mixed batch (2000 req/s, 8 slots): splitting host copies into 8 MiB pieces, or capping
+// the requests with large copies running at once, lengthened the tails and cut the
+// saturated throughput (198 -> 121-162 GB/s), so copies go out whole and nothing is capped.
 constexpr uint32_t kAdmitWindow = 64;
 
 }  // namespace
@@ -151,7 +135,6 @@ struct fz_server {
     std::deque<fz_completion>  done;   // finished but not yet handed out
     std::atomic<uint32_t>      ndone{0};  // done.size(), read without the lock by poll
     uint32_t                   running = 0;
-    uint32_t                   running_large = 0, max_large = 1;  // large host-buffer requests
     std::atomic<bool>          stop{false};
     std::vector<std::thread>   workers;
 };
@@ -190,7 +173,6 @@ void finish(fz_server* S, Slot& sl, fz_status st, uint64_t result)
     S->done.push_back(fz_completion{sl.req.id, st, result});
     S->ndone.store((uint32_t)S->done.size(), std::memory_order_release);
     --S->running;
-    if (sl.large) --S->running_large, sl.large = false;
     sl.phase = Phase::Idle;
 }
 
@@ -203,7 +185,8 @@ fz_status issue_decompress(fz_server* S, Slot& sl, const fz_header& h)
     float*      d_dst = reinterpret_cast<float*>(dev ? sl.req.dst : S->d_pool + sl.dst_off);
     if (4 * h.n > sl.req.dst_capacity) return FZ_OUT_OF_SPACE;
     fz_status st = fz_decompress(sl.ws, d_src, sl.req.src_bytes, &h, d_dst, h.n, reinterpret_cast<fz_stream_t>(sl.stream));
-    if (st == FZ_SUCCESS && !dev && copy_pieces(sl.req.dst, d_dst, 4 * h.n, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+    if (st == FZ_SUCCESS && !dev &&
+        cudaMemcpyAsync(sl.req.dst, d_dst, 4 * h.n, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
         st = FZ_FAIL_GPU_MEMCPY;
     if (st == FZ_SUCCESS && cudaMemcpyAsync(sl.h_buf + 64, sl.ws->status, 4, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
         st = FZ_FAIL_GPU_MEMCPY;
@@ -223,7 +206,7 @@ void issue(fz_server* S, Slot& sl, const fz_request& r, uint64_t src_off, uint64
     uint8_t*    d_dst = dev ? (uint8_t*)r.dst : S->d_pool + dst_off;
     fz_stream_t hs    = reinterpret_cast<fz_stream_t>(sl.stream);
     fz_status   st    = FZ_SUCCESS;
-    if (!dev && copy_pieces(d_src, r.src, src_b, cudaMemcpyHostToDevice, sl.stream) != cudaSuccess)
+    if (!dev && cudaMemcpyAsync(d_src, r.src, src_b, cudaMemcpyHostToDevice, sl.stream) != cudaSuccess)
         st = FZ_FAIL_GPU_MEMCPY;
     if (r.dir == FZ_COMPRESS) {
         if (st == FZ_SUCCESS)
@@ -302,7 +285,7 @@ bool retire(fz_server* S, Slot& sl)
             finish(S, sl, st, st == FZ_SUCCESS ? bytes : 0);
             return true;
         }
-        if (copy_pieces(sl.req.dst, S->d_pool + sl.dst_off, bytes, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+        if (cudaMemcpyAsync(sl.req.dst, S->d_pool + sl.dst_off, bytes, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
             st = FZ_FAIL_GPU_MEMCPY;
         if (st == FZ_SUCCESS && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) st = FZ_FAIL_GPU_ILLEGAL_ACCESS;
         if (st != FZ_SUCCESS) {
@@ -318,8 +301,8 @@ bool retire(fz_server* S, Slot& sl)
 }
 
 // Admits a queued request onto an idle slot: the first one among the first kAdmitWindow
-// queue entries that may start (see kLargeBytes) and whose buffers the pool can hold;
-// requests that can never run complete at once with an error.  The request is issued
+// queue entries whose buffers the pool can hold; requests that can never run complete at
+// once with an error.  The request is issued
 // outside the lock.  Returns true when something was admitted or rejected.
 bool admit(fz_server* S, Slot& sl)
 {
@@ -327,7 +310,7 @@ bool admit(fz_server* S, Slot& sl)
     uint64_t   so = 0, sb = 0, dof = 0, db = 0;
     {
         std::lock_guard<std::mutex> lk(S->mu);
-        bool                        changed = false, large_blocked = false;
+        bool                        changed = false;
         uint32_t                    k       = 0;
         for (;;) {
             if (k >= S->queue.size() || k >= kAdmitWindow) return changed;
@@ -347,28 +330,17 @@ bool admit(fz_server* S, Slot& sl)
                 changed = true;
                 continue;
             }
-            const bool large = !is_device(r) && sb + db > kLargeBytes;
-            // large ones keep their order: once one is blocked, later large ones wait too
-            if (large && (large_blocked || S->running_large >= S->max_large)) {
-                large_blocked = true;
-                ++k;
-                continue;
-            }
-            if (!S->pool->alloc(sb, &so)) {  // wait for memory to free up
-                large_blocked |= large;
+            if (!S->pool->alloc(sb, &so)) {  // it waits for memory to free up; a later one may fit
                 ++k;
                 continue;
             }
             if (!S->pool->alloc(db, &dof)) {
                 S->pool->release(so, sb);
-                large_blocked |= large;
                 ++k;
                 continue;
             }
             sl.hdr = qf.h;
             if (qf.has_header) r.header = &sl.hdr;
-            sl.large = large;
-            if (large) ++S->running_large;
             S->queue.erase(S->queue.begin() + k);
             ++S->running;
             break;
@@ -431,7 +403,6 @@ fz_status fz_server_create(uint64_t hbm_budget, uint32_t slots, uint64_t max_n, 
             return st;
         }
     }
-    S->max_large      = std::max(1u, slots / 4);
     const uint32_t nw = std::min(kWorkers, slots);
     for (uint32_t k = 0; k < nw; ++k) S->workers.emplace_back(worker, S, k, nw);
     *out = S;

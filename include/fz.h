@@ -380,10 +380,7 @@ typedef struct fz_completion {
    requests and admit queued ones as slots and pool memory free up, so requests that arrive
    while others run overlap on the device; fz_server_poll (non-blocking) hands out the
    completions.  Admission looks at the first 64 queued requests: one may start ahead of
-   earlier ones that cannot (pool memory, or the cap of max(1, slots/4) host-buffer requests
-   with more than 32 MiB of copies running at once -- those keep their order among
-   themselves), and host copies go out in 8 MiB pieces so that small requests' copies are
-   not held behind a large one's.  The functions may be called from any thread.  No counterpart in the
+   earlier ones that wait for pool memory.  The functions may be called from any thread.  No counterpart in the
    reference (one field per process, fz.cu:226-238). */
 typedef struct fz_server fz_server;
 fz_status fz_server_create(uint64_t hbm_budget, uint32_t slots, uint64_t max_n, fz_server** out);
