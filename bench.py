@@ -50,6 +50,8 @@ FIELDS = {
     "exafel": ((39200, 388, 1), 1e-3, "peaks2d", "exafel-like 39200x388 f32 (peaks on N(0,0.5) background), relative eb 1e-3"),
     "cesm": ((3600, 1800, 1), 1e-3, "smooth2d", "cesm-like 3600x1800 f32 (smooth, ~30% zeros), relative eb 1e-3"),
     "hurricane": ((500, 500, 100), 1e-3, "smooth3d", "hurricane-like 500x500x100 f32 (smooth 3D, ~40% zeros), relative eb 1e-3"),
+    "exafel_u": ((39201, 388, 1), 1e-3, "peaks2d", "exafel-like 39201x388 f32 (rows not a multiple of 4), relative eb 1e-3"),
+    "oned": ((1 << 25, 1, 1), 1e-3, "smooth1d", "1D 2^25 f32 (smooth series with zero runs), relative eb 1e-3"),
 }
 DIMS, EB, KIND, WORKLOAD = FIELDS["exafel"]
 METRIC = "compress/decompress GB/s + %HBM peak"
@@ -66,9 +68,10 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--quick", action="store_true", help="headline only: no per-dimensionality, batch or serving keys")
-    p.add_argument("--workload", choices=["exafel", "batch", "serving"], default="exafel",
+    p.add_argument("--workload", choices=["exafel", "batch", "serving", "kernels"], default="exafel",
                    help="exafel: the headline line (single-field workload, see --field); batch: 512 mixed "
-                        "1D/2D/3D fields batched vs per field; serving: a Poisson request trace")
+                        "1D/2D/3D fields batched vs per field; serving: a Poisson request trace; kernels: "
+                        "every kernel kind on the --field workload, --steps times (for a profiler)")
     p.add_argument("--field", choices=sorted(FIELDS), default="exafel",
                    help="the single-field workload of the headline line (default exafel)")
     p.add_argument("--batch-fields", type=int, default=512)
@@ -828,6 +831,42 @@ def run_serving(args, local_rank):
     return out
 
 
+def run_kernels(args, local_rank):
+    """Every kernel kind once per step on one --field field: compression (range, encode,
+    compaction), decompression of the sidecar stream, decompression of a COMPAT stream
+    (block offsets first), and the no-allocation compression (the look-back kernel), each
+    checked against the workspace path's bytes.  Prints one line of launches per kind."""
+    import torch
+    import __graft_entry__ as g
+    fz = g.load_package()
+    torch.cuda.set_device(local_rank)
+    f = make_fields(1, 1)[0]
+    x = torch.from_numpy(f).cuda()
+    n = x.numel()
+    ws = fz.Workspace(n)
+    caps = {m: fz.max_compressed_bytes(n, DIMS, m) for m in (fz.MODE_SIDECAR, fz.MODE_COMPAT)}
+    out = {m: torch.empty(caps[m], dtype=torch.uint8, device="cuda") for m in caps}
+    y = torch.empty(n, dtype=torch.float32, device="cuda")
+    na = torch.empty(caps[fz.MODE_SIDECAR], dtype=torch.uint8, device="cuda")
+    noalloc = n <= (1 << 26)
+    for _ in range(args.steps):
+        for m in (fz.MODE_SIDECAR, fz.MODE_COMPAT):
+            st = fz.compress(x, DIMS, EB, mode=m, ws=ws, out=out[m])
+            fz.decompress(st, ws=ws, out=y)
+        if noalloc:
+            nb = C.c_uint64()
+            fz._check("fz_compress_noalloc", fz.lib().fz_compress_noalloc(
+                C.c_void_p(x.data_ptr()), n, fz._dims(DIMS), EB, fz.EB_REL, fz.MODE_SIDECAR,
+                C.c_void_p(na.data_ptr()), na.numel(), C.byref(nb), fz._stream_handle(None)))
+            assert torch.equal(na[: nb.value], out[fz.MODE_SIDECAR][: nb.value])
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": WORKLOAD, "steps": args.steps,
+                      "per_step": ["k_range_fields", "k_encode_fields", "k_compact_fields", "k_decompress (sidecar)",
+                                   "k_range_fields", "k_encode_fields", "k_compact_fields", "k_offsets",
+                                   "k_decompress (COMPAT)"] + (["k_range", "k_compress"] if noalloc else [])}),
+          flush=True)
+
+
 def main():
     global DIMS, EB, KIND, WORKLOAD
     args = parse_args()
@@ -841,6 +880,9 @@ def main():
     elif args.workload == "serving":
         if rank == 0:
             print(json.dumps(run_serving(args, local_rank)), flush=True)
+    elif args.workload == "kernels":
+        if rank == 0:
+            run_kernels(args, local_rank)
     else:
         run_fz(args, rank, world, local_rank)
 
