@@ -1,17 +1,18 @@
 // fz_compress.cu -- compression kernels.
 //
-//   k_range       max - min of the field and the error-bound constants (fz.cu:137,
-//                 lorenzo_var.cuh:562-563), one pass.
-//   k_encode      Lorenzo dual-quantisation (lorenzo_var.cuh:47-295), bitshuffle +
-//                 chunk flags + bitmap (fz.cu:61-111) and each block's non-zero chunks
-//                 compacted into its own slot (encodeDebug, fz.cu:49-59); independent
-//                 CTAs, one 2048-code shuffle block per warp.
-//   k_compact     the prefix sum over the blocks' chunk counts (replacing
-//                 cub::DeviceScan, fz.cu:187-201) from per-group sums, the move of
-//                 the chunks to their final offsets, the offset table and the header.
-//   k_compress    the same forward path in a single launch with a decoupled look-back
-//                 over scan tiles (persistent, software pipelined); used where no
-//                 scratch for the slots exists (fz_compress_noalloc).
+//   k_range_fields    max/min of 16384-element chunks of a list of fields (fz.cu:137),
+//                     the error-bound constants following from them (lorenzo_var.cuh:
+//                     562-563).
+//   k_encode_fields   Lorenzo dual-quantisation (lorenzo_var.cuh:47-295), bitshuffle +
+//                     chunk flags + bitmap (fz.cu:61-111) and each block's non-zero chunks
+//                     compacted into its own slot (encodeDebug, fz.cu:49-59); independent
+//                     CTAs, one 2048-code shuffle block per warp.
+//   k_compact_fields  the prefix sum over the blocks' chunk counts (replacing
+//                     cub::DeviceScan, fz.cu:187-201) from per-group sums, the move of the
+//                     chunks to their final offsets, the offset table and the header.
+//   k_range, k_compress  the same forward path with a decoupled look-back over scan
+//                     tiles in a single persistent launch after a range pass; used where no
+//                     scratch for the slots exists (fz_compress_noalloc).
 //
 // Work decomposition: one warp owns one 2048-code shuffle block.  The warp computes its
 // codes from the floats (halo rows come from L2), stages them in 4 KiB of shared memory,
@@ -1144,15 +1145,6 @@ constexpr uint32_t kCompactBlocks = 32;   // shuffle blocks per compaction item
 constexpr int      kEncodeRing    = FZ_ENCODE_RING;  // group rows in flight per warp (1D/2D)
 constexpr int      kEncodeCtas    = FZ_ENCODE_CTAS;  // CTAs per SM the 1D/2D encode kernels are built for
 
-// Sum of v over the CTA (256 threads), in every thread.
-__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red)
-{
-    v = __reduce_add_sync(kFull, v);
-    __syncthreads();  // red may still be read by a previous call
-    if ((threadIdx.x & 31u) == 0) red[threadIdx.x >> 5] = v;
-    __syncthreads();
-    return __reduce_add_sync(kFull, (threadIdx.x & 31u) < kCompressWarps ? red[threadIdx.x & 31u] : 0u);
-}
 
 // ---------------------------------------------------------------- items --
 constexpr uint32_t kCtlOverflow    = 1u << 8;                    // FieldCtl::flags: some code overflowed
@@ -1164,7 +1156,7 @@ void field_items(uint32_t n, uint32_t nb, uint32_t ntiles, bool rel, uint32_t& n
 {
     nr = rel ? (uint32_t)std::max<uint64_t>(1, cdiv(n, kRangeItemElems)) : 0u;
     ne = (uint32_t)cdiv(ntiles, kCompressWarps);
-    nc = (uint32_t)std::max<uint64_t>(1, cdiv(nb, kCompactBlocks));
+    nc = (uint32_t)cdiv(nb, kCompactBlocks);  // none without full blocks (the encode launch writes the header)
 }
 
 // Item k of a list launch: field f owns items [segs[f].start, segs[f].start + segs[f].count)
@@ -1233,9 +1225,13 @@ __device__ __forceinline__ void range_item(const FieldJob& J, uint32_t i, uint32
 
 // Encode item i of field J: scan tile ne-1-i (the last tile first: the range launch read
 // the field front to back, so its end is the part most likely still in L2), one shuffle
-// block per warp; r = ebx2_r.
+// block per warp; r = ebx2_r; par = this call's group-sum set, also kept in bit 31 of each
+// block's count for the compaction launch.
+constexpr uint32_t kCountPar = 1u << 31;
+
 template <int ND, int kRing>
-__device__ __forceinline__ void encode_item(const FieldJob& J, uint32_t i, float r, uint32_t* sm, float4* ring)
+__device__ __forceinline__ void encode_item(const FieldJob& J, uint32_t i, float r, uint32_t par, uint32_t* sm,
+                                            float4* ring)
 {
     const uint32_t      lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     const CompressArgs& a    = J.a;
@@ -1256,95 +1252,101 @@ __device__ __forceinline__ void encode_item(const FieldJob& J, uint32_t i, float
             pre += __popc(bm[k]);
         }
         if (lane == 0) {
-            J.counts[t] = cnt;
-            if (cnt) atomicAdd(J.supers + t / kSuperBlocks, cnt);
+            J.counts[t] = cnt | (par ? kCountPar : 0u);
+            if (cnt) atomicAdd(J.supers + par * J.sstride + t / kSuperBlocks, cnt);
         }
     }
     if (ovf && lane == 0) atomicOr(&J.ctl->flags, kCtlOverflow);
 }
 
+// The header of field J with `total` chunks, the offset table's total, and the control
+// words restored for the next call (one thread; after every encode item of the call).
+__device__ void finish_field(const FieldJob& J, uint32_t total)
+{
+    const CompressArgs& a  = J.a;
+    FieldCtl*           C  = J.ctl;
+    const EbInfo        eb = J.rel ? eb_from_range(ord2f(__ldcg(C->mm)), ord2f(__ldcg(C->mm + 1)), a.eb_rel) : a.ebh;
+    const uint32_t      cf = __ldcg(&C->flags);
+    write_header(a, eb, ((cf & kCtlOverflow) ? 1u : 0u) | ((cf & kStatusNonfinite) ? 2u : 0u), total);
+    if (a.boff) {
+        a.boff[a.nb] = total;  // the total closes the offset table; zero its 16-byte pad
+        for (uint32_t k = a.nb + 1; k < (uint32_t)(pad16(4ull * (a.nb + 1)) / 4); ++k) a.boff[k] = 0;
+    }
+    C->mm[0] = 0xFFFFFFFFu, C->mm[1] = 0u;
+    C->flags = 0;
+    if (a.mirror) {
+        // header and status in one place, so a caller reads both with one copy
+        __threadfence();
+        const uint4* h = reinterpret_cast<const uint4*>(a.out);
+        uint4*       m = reinterpret_cast<uint4*>(a.mirror);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) m[k] = __ldcg(h + k);
+        a.mirror[16] = __ldcg(a.status);
+    }
+}
+
 // Compaction item i of field J: blocks [32 i, 32 i + 32), four per warp, each warp on its
-// own (no CTA barrier until the item's end).  A warp's first chunk offset is the sum of
-// the group sums (kSuperBlocks blocks each) before its group plus the counts of the blocks of its
-// group before its own; then it writes the offset table entries of its 4 blocks and moves
-// their chunks from the slots to Section B (output chunk q of the warp comes from the last
-// of its blocks whose prefix is <= q; 16-byte loads, four in flight per lane).  The field's
-// last item to finish writes the header and restores the field's control words.  No other
-// CTA reads what a compaction CTA writes, so the items need no memory fences.
+// own.  A warp's first chunk offset is the sum of this call's group sums (kSuperBlocks
+// blocks each) before its group plus the counts of the blocks of its group before its own;
+// then it writes the offset table entries of its 4 blocks and moves their chunks from the
+// slots to Section B (output chunk q of the warp comes from the last of its blocks whose
+// prefix is <= q; 16-byte loads, four in flight per lane).  The call's group-sum set is
+// the parity bit of the counts; the warps clear the other set for the next call.  The warp
+// holding the last block knows the total: it writes the header and advances the call
+// counter.  No CTA reads what another compaction CTA writes: no barrier, fence or atomic.
 constexpr uint32_t kCompactWarpBlocks = kCompactBlocks / kCompressWarps;  // 4
 
-__device__ __forceinline__ void compact_item(const FieldJob& J, uint32_t i, uint32_t* s_red1, uint32_t* s_last)
+__device__ __forceinline__ void compact_item(const FieldJob& J, uint32_t i)
 {
-    const uint32_t      tid = threadIdx.x, lane = tid & 31u, wid = tid >> 5;
-    const CompressArgs& a   = J.a;
-    const uint32_t      b0  = i * kCompactBlocks + wid * kCompactWarpBlocks, sup = b0 / kSuperBlocks;
-    if (b0 < a.nb) {
-        static_assert(kSuperBlocks <= 64, "counts before a warp's blocks in its group: two per lane");
-        uint32_t acc = 0;
-        for (uint32_t k = lane; k < sup; k += 32) acc += __ldcg(J.supers + k);
-        const uint32_t g0 = sup * kSuperBlocks;
-        if (g0 + lane < b0) acc += __ldcg(J.counts + g0 + lane);
-        if (g0 + 32 + lane < b0) acc += __ldcg(J.counts + g0 + 32 + lane);
-        const uint32_t c   = lane < kCompactWarpBlocks && b0 + lane < a.nb ? __ldcg(J.counts + b0 + lane) : 0u;
-        const uint32_t exc = __reduce_add_sync(kFull, acc);
-        // inclusive prefix of the 4 counts in lanes 0..3
-        uint32_t v = c;
+    const uint32_t      lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const CompressArgs& a    = J.a;
+    const uint32_t      gw = i * kCompressWarps + wid;  // warp of the launch's items of this field
+    const uint32_t      b0 = gw * kCompactWarpBlocks, sup = b0 / kSuperBlocks;
+    // the call's set: the parity bit of any count of this call (block 0's); every warp of the
+    // field's items, past the last block too, clears its share of the other set
+    const uint32_t  par = __ldcg(J.counts) >> 31;
+    const uint32_t* set = J.supers + par * J.sstride;
+    uint32_t*       old = J.supers + (par ^ 1u) * J.sstride;
+    for (uint32_t k = gw * 32 + lane; k < J.sstride; k += J.nc * kCompressWarps * 32) old[k] = 0;
+    if (b0 >= a.nb) return;
+    static_assert(kSuperBlocks <= 64, "counts before a warp's blocks in its group: two per lane");
+    uint32_t acc = 0;
+    for (uint32_t k = lane; k < sup; k += 32) acc += __ldcg(set + k);
+    const uint32_t g0 = sup * kSuperBlocks;
+    if (g0 + lane < b0) acc += __ldcg(J.counts + g0 + lane) & ~kCountPar;
+    if (g0 + 32 + lane < b0) acc += __ldcg(J.counts + g0 + 32 + lane) & ~kCountPar;
+    const uint32_t c = lane < kCompactWarpBlocks && b0 + lane < a.nb ? __ldcg(J.counts + b0 + lane) & ~kCountPar : 0u;
+    const uint32_t exc = __reduce_add_sync(kFull, acc);
+    // inclusive prefix of the 4 counts in lanes 0..3
+    uint32_t v = c;
 #pragma unroll
-        for (uint32_t o = 1; o < kCompactWarpBlocks; o <<= 1) {
-            const uint32_t u = __shfl_up_sync(kFull, v, o);
-            if (lane >= o) v += u;
-        }
-        if (a.boff && lane < kCompactWarpBlocks && b0 + lane < a.nb) a.boff[b0 + lane] = exc + v - c;
-        const uint32_t p1 = __shfl_sync(kFull, v - c, 1), p2 = __shfl_sync(kFull, v - c, 2);
-        const uint32_t p3 = __shfl_sync(kFull, v - c, 3), tot = __shfl_sync(kFull, v, 3);
-        uint4*         B  = reinterpret_cast<uint4*>(a.out + a.off_b) + exc;
-        for (uint32_t q0 = lane; q0 < tot; q0 += 4 * 32) {
-            uint4 val[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const uint32_t q = q0 + u * 32;
-                if (q < tot) {
-                    const uint32_t j  = (q >= p1) + (q >= p2) + (q >= p3);  // blocks with no chunks never match last
-                    const uint32_t pj = j == 0 ? 0u : j == 1 ? p1 : j == 2 ? p2 : p3;
-                    val[u]            = __ldcg(J.slots + (size_t)(b0 + j) * kChunks + (q - pj));
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (q0 + u * 32 < tot) B[q0 + u * 32] = val[u];
-        }
+    for (uint32_t o = 1; o < kCompactWarpBlocks; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(kFull, v, o);
+        if (lane >= o) v += u;
     }
-    // the field's last item to finish: header, offset-table total, resets
-    __syncthreads();
-    if (tid == 0) *s_last = atomicAdd(&J.ctl->c_done, 1u) == J.nc - 1;
-    __syncthreads();
-    if (!*s_last) return;
-    __threadfence();  // the other items' counts of c_done came before: the group sums are final
-    const uint32_t nsup    = (uint32_t)cdiv(a.nb, kSuperBlocks);
-    uint32_t       total_c = 0;
-    for (uint32_t k = tid; k < nsup; k += blockDim.x) total_c += __ldcg(J.supers + k);
-    total_c = block_sum(total_c, s_red1);
-    for (uint32_t k = tid; k < nsup; k += blockDim.x) J.supers[k] = 0;
-    if (tid == 0) {
-        FieldCtl*      C  = J.ctl;
-        const EbInfo   eb = J.rel ? eb_from_range(ord2f(__ldcg(C->mm)), ord2f(__ldcg(C->mm + 1)), a.eb_rel) : a.ebh;
-        const uint32_t cf = __ldcg(&C->flags);
-        write_header(a, eb, ((cf & kCtlOverflow) ? 1u : 0u) | ((cf & kStatusNonfinite) ? 2u : 0u), total_c);
-        if (a.boff) {
-            a.boff[a.nb] = total_c;  // the total closes the offset table; zero its 16-byte pad
-            for (uint32_t k = a.nb + 1; k < (uint32_t)(pad16(4ull * (a.nb + 1)) / 4); ++k) a.boff[k] = 0;
-        }
-        C->mm[0] = 0xFFFFFFFFu, C->mm[1] = 0u;
-        C->c_done = 0, C->flags = 0;
-        if (a.mirror) {
-            // header and status in one place, so a caller reads both with one copy
-            __threadfence();
-            const uint4* h = reinterpret_cast<const uint4*>(a.out);
-            uint4*       m = reinterpret_cast<uint4*>(a.mirror);
+    if (a.boff && lane < kCompactWarpBlocks && b0 + lane < a.nb) a.boff[b0 + lane] = exc + v - c;
+    const uint32_t p1 = __shfl_sync(kFull, v - c, 1), p2 = __shfl_sync(kFull, v - c, 2);
+    const uint32_t p3 = __shfl_sync(kFull, v - c, 3), tot = __shfl_sync(kFull, v, 3);
+    uint4*         B  = reinterpret_cast<uint4*>(a.out + a.off_b) + exc;
+    for (uint32_t q0 = lane; q0 < tot; q0 += 4 * 32) {
+        uint4 val[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) m[k] = __ldcg(h + k);
-            a.mirror[16] = __ldcg(a.status);
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t q = q0 + u * 32;
+            if (q < tot) {
+                const uint32_t j  = (q >= p1) + (q >= p2) + (q >= p3);  // blocks with no chunks never match last
+                const uint32_t pj = j == 0 ? 0u : j == 1 ? p1 : j == 2 ? p2 : p3;
+                val[u]            = __ldcg(J.slots + (size_t)(b0 + j) * kChunks + (q - pj));
+            }
         }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (q0 + u * 32 < tot) B[q0 + u * 32] = val[u];
+    }
+    if (lane == 0 && b0 + kCompactWarpBlocks >= a.nb) {
+        // the last block's warp: every count is in, so the total is exc + tot
+        finish_field(J, exc + tot);
+        J.ctl->epoch += 1u;  // the next call uses the set cleared here
     }
 }
 
@@ -1388,21 +1390,29 @@ __global__ void __launch_bounds__(kCompressWarps * 32, encode_ctas<ND>())
     float4*       ring = kR ? reinterpret_cast<float4*>(esm + kCompressWarps * kBlockWords) + (threadIdx.x >> 5) * kR * 64
                             : nullptr;
     __shared__ float    s_r;
-    __shared__ uint32_t s_rf;
+    __shared__ uint32_t s_rf, s_par;
     if (threadIdx.x == 0) s_rf = 0xFFFFFFFFu;
     for (uint32_t k = blockIdx.x; k < total; k += gridDim.x) {
         uint32_t f = 0, i = k;
         if (kList) locate(segs, nseg, k, f, i);
         const FieldJob& J = kList ? jobs[f] : one;
         if (threadIdx.x == 0 && s_rf != f) {
-            // ebx2_r of the field: from its range (relative eb; the range launch has finished)
-            s_r  = J.rel ? eb_from_range(ord2f(__ldcg(J.ctl->mm)), ord2f(__ldcg(J.ctl->mm + 1)), J.a.eb_rel).ebx2_r
-                         : J.a.ebh.ebx2_r;
-            s_rf = f;
+            // ebx2_r of the field: from its range (relative eb; the range launch has finished);
+            // the call's group-sum set (the compaction launch moves the counter on)
+            s_r   = J.rel ? eb_from_range(ord2f(__ldcg(J.ctl->mm)), ord2f(__ldcg(J.ctl->mm + 1)), J.a.eb_rel).ebx2_r
+                          : J.a.ebh.ebx2_r;
+            s_par = __ldcg(&J.ctl->epoch) & 1u;
+            s_rf  = f;
         }
         __syncthreads();
-        encode_item<ND, kR>(J, i, s_r, smem, ring);
+        encode_item<ND, kR>(J, i, s_r, s_par, smem, ring);
         __syncthreads();  // the blocks' shared images before the next item
+        // a field without full shuffle blocks has one encode item and no compaction: the
+        // header is written here (its counter stays, no group sums were used)
+        if (J.a.nb == 0 && threadIdx.x == 0) {
+            __threadfence();
+            finish_field(J, 0u);
+        }
     }
 }
 
@@ -1410,12 +1420,10 @@ template <bool kList>
 __global__ void __launch_bounds__(256) k_compact_fields(const FieldJob* __restrict__ jobs, const Segment* __restrict__ segs,
                                                         uint32_t nseg, uint32_t total, const __grid_constant__ FieldJob one)
 {
-    __shared__ uint32_t s_red[kCompressWarps], s_last;
     for (uint32_t k = blockIdx.x; k < total; k += gridDim.x) {
         uint32_t f = 0, i = k;
         if (kList) locate(segs, nseg, k, f, i);
-        compact_item(kList ? jobs[f] : one, i, s_red, &s_last);
-        __syncthreads();
+        compact_item(kList ? jobs[f] : one, i);
     }
 }
 

@@ -58,15 +58,16 @@ struct CompressArgs {
 // compaction), each a persistent grid striding over the list's items: range items (a
 // 16384-element chunk's max/min, relative eb only), encode items (8 shuffle blocks:
 // codes, bitshuffle, flags, chunks into per-block slots) and compaction items (32 blocks:
-// offsets, chunks to their final place; a field's last one writes its header).  One field
-// is a list of one, passed as a kernel parameter.
+// offsets, chunks to their final place; the warp holding the last block writes the
+// header).  One field is a list of one, passed as a kernel parameter.
 
-// Per-field control words (device, 32 bytes).  Between calls: mm = {0xFFFFFFFF, 0}, the
-// rest 0 -- the field's last compaction item restores that.
+// Per-field control words (device, 32 bytes).  Between calls: mm = {0xFFFFFFFF, 0},
+// flags 0 -- restored by whoever writes the header -- and epoch = the number of calls
+// that had full shuffle blocks.
 struct FieldCtl {
     uint32_t mm[2];    // range accumulators (order-preserving u32)
-    uint32_t c_done;   // finished compaction items
     uint32_t flags;    // this call: kStatusNonfinite, bit 8 code overflow
+    uint32_t epoch;    // a call uses group-sum set (epoch & 1) and clears the other
     uint32_t pad[4];
 };
 
@@ -75,7 +76,9 @@ struct FieldJob {
     FieldCtl*    ctl;
     uint4*       slots;   // 4 KiB per shuffle block
     uint32_t*    counts;  // chunks per block
-    uint32_t*    supers;  // chunks per group of kSuperBlocks blocks (zero on entry, left zero)
+    uint32_t*    supers;  // two sets of `sstride` words: chunks per group of kSuperBlocks
+                          // blocks; a call adds into one set and clears the other
+    uint32_t     sstride;     // words per set (at least the field's groups)
     uint32_t     nr, ne, nc;  // range, encode, compaction items
     uint32_t     rel;         // relative eb: the eb follows from the range items
 };
