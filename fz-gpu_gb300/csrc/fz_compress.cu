@@ -1,6 +1,6 @@
 // fz_compress.cu -- compression kernels.
 //
-//   k_range_fields    max/min of 16384-element chunks of a list of fields (fz.cu:137),
+//   k_range_fields    max/min of 1024-element items of a list of fields (fz.cu:137),
 //                     the error-bound constants following from them (lorenzo_var.cuh:
 //                     562-563).
 //   k_encode_fields   Lorenzo dual-quantisation (lorenzo_var.cuh:47-295), bitshuffle +
@@ -30,11 +30,14 @@
 #ifndef FZ_RANGE_VEC
 #define FZ_RANGE_VEC 8
 #endif
-#ifndef FZ_RANGE_ROUNDS
-#define FZ_RANGE_ROUNDS 2
-#endif
 #ifndef FZ_ENCODE_CTAS
 #define FZ_ENCODE_CTAS 3
+#endif
+#ifndef FZ_ENCODE_CTAS_2D
+#define FZ_ENCODE_CTAS_2D 5
+#endif
+#ifndef FZ_RANGE_CTAS
+#define FZ_RANGE_CTAS 5
 #endif
 
 namespace fz {
@@ -1130,7 +1133,8 @@ __global__ void __launch_bounds__(kCompressWarps * 32, 3) k_compress(const Compr
 // ================================================ list compression ==
 // Compression of a list of fields in three launches, each a persistent grid striding over
 // a device work list (FieldJob / Segment, fz_internal.h):
-//   k_range_fields     range items: max/min of a 16384-element chunk (relative eb)
+//   k_range_fields     range items: max/min of 1024 elements (relative eb); each CTA a
+//                      contiguous run of items, one reduction per field it touches
 //   k_encode_fields    encode items: 8 shuffle blocks, one per warp -- codes, bitshuffle,
 //                      chunk flags, bitmap words, sidecar, the block's non-zero chunks
 //                      compacted into its own 4 KiB slot, its count into counts[] and the
@@ -1148,9 +1152,8 @@ constexpr int      kEncodeCtas    = FZ_ENCODE_CTAS;  // CTAs per SM the 1D/2D en
 
 // ---------------------------------------------------------------- items --
 constexpr uint32_t kCtlOverflow    = 1u << 8;                    // FieldCtl::flags: some code overflowed
-constexpr uint32_t kRangeVec       = FZ_RANGE_VEC;               // 16-byte loads in flight per thread
-constexpr uint32_t kRangeRounds    = FZ_RANGE_ROUNDS;            // rounds per range item
-constexpr uint32_t kRangeItemElems = 256 * kRangeVec * 4 * kRangeRounds;  // 16384
+constexpr uint32_t kRangeBatch     = FZ_RANGE_VEC;  // range items (16-byte loads) in flight per thread
+constexpr uint32_t kRangeItemElems = 256 * 4;       // one 16-byte load per thread
 
 void field_items(uint32_t n, uint32_t nb, uint32_t ntiles, bool rel, uint32_t& nr, uint32_t& ne, uint32_t& nc)
 {
@@ -1174,41 +1177,24 @@ __device__ __forceinline__ void locate(const Segment* __restrict__ segs, uint32_
     i = k - __ldg(&segs[lo].start);
 }
 
-// Range item i: max/min of elements [i*16384, (i+1)*16384) (the last item also takes the
-// n mod 4 elements past the 16-byte loads) folded into the field's accumulators.
-__device__ __forceinline__ void range_item(const FieldJob& J, uint32_t i, uint32_t (*sred)[kCompressWarps])
+// Range items: 1024 elements each (one 16-byte load per thread).  A CTA takes a contiguous
+// run of items -- CTA c of G the items [c T / G, (c + 1) T / G) of a launch over T items --
+// so runs differ by at most one item, and keeps kRangeBatch loads per thread in flight.  The
+// running max/min of a thread is carried across its items and folded into the field's
+// accumulators once per field the run touches.
+__device__ __forceinline__ void range_flush(const FieldJob& J, float mn, float mx, uint32_t nonfinite,
+                                            uint32_t (*sred)[kCompressWarps])
 {
-    const float*   in = J.a.in;
-    const uint32_t n = J.a.n, n4 = n / 4, tid = threadIdx.x;
-    float          mn = INFINITY, mx = -INFINITY;
-#pragma unroll 1
-    for (uint32_t rd = 0; rd < kRangeRounds; ++rd) {
-        const uint32_t b0 = i * (kRangeItemElems / 4) + rd * (256 * kRangeVec) + tid;
-        float4         v[kRangeVec];
-#pragma unroll
-        for (uint32_t k = 0; k < kRangeVec; ++k)
-            if (b0 + k * 256 < n4) v[k] = ldg4(in + 4 * (size_t)(b0 + k * 256));
-#pragma unroll
-        for (uint32_t k = 0; k < kRangeVec; ++k) {
-            if (b0 + k * 256 >= n4) continue;
-            mn = fmin_nan(fmin_nan(mn, v[k].x), fmin_nan(v[k].y, fmin_nan(v[k].z, v[k].w)));
-            mx = fmax_nan(fmax_nan(mx, v[k].x), fmax_nan(v[k].y, fmax_nan(v[k].z, v[k].w)));
-        }
-    }
-    // NaN leaves both NaN; -Inf shows in the min, +Inf in the max
-    uint32_t nonfinite = (mn != mn) | (mn == -INFINITY) | (mx == INFINITY);
-    if ((i + 1) * kRangeItemElems >= n && tid < n - 4 * n4) {
-        const float v = in[4 * n4 + tid];
-        mn = fminf(mn, v), mx = fmaxf(mx, v);
-        nonfinite |= !isfinite(v);
-    }
+    // NaN leaves both NaN; -Inf shows in the min, +Inf in the max (the start values +Inf /
+    // -Inf of a thread without elements stay on the other side)
+    nonfinite |= (mn != mn) | (mn == -INFINITY) | (mx == INFINITY);
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
         mn = fminf(mn, __shfl_xor_sync(kFull, mn, o));
         mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
     }
     nonfinite = __reduce_or_sync(kFull, nonfinite);
-    const uint32_t lane = tid & 31u, wid = tid >> 5;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, wid = tid >> 5;
     if (lane == 0) sred[0][wid] = f2ord(mn), sred[1][wid] = f2ord(mx), sred[2][wid] = nonfinite;
     __syncthreads();
     if (tid < 32) {
@@ -1220,6 +1206,32 @@ __device__ __forceinline__ void range_item(const FieldJob& J, uint32_t i, uint32
             atomicMax(J.ctl->mm + 1, c);
             if (f) atomicOr(J.a.status, kStatusNonfinite), atomicOr(&J.ctl->flags, kStatusNonfinite);
         }
+    }
+    __syncthreads();  // sred before the next flush
+}
+
+// Items [i, i + cnt) of field J (cnt <= kRangeBatch) into the thread's running max/min; the
+// field's last item also takes the n mod 4 elements past its 16-byte loads.
+__device__ __forceinline__ void range_items(const FieldJob& J, uint32_t i, uint32_t cnt, float& mn, float& mx,
+                                            uint32_t& nonfinite)
+{
+    const float*   in = J.a.in;
+    const uint32_t n = J.a.n, n4 = n / 4, tid = threadIdx.x;
+    const uint32_t q0 = i * (kRangeItemElems / 4) + tid;
+    float4         v[kRangeBatch];
+#pragma unroll
+    for (uint32_t k = 0; k < kRangeBatch; ++k)
+        if (k < cnt && q0 + k * 256 < n4) v[k] = ldg4(in + 4 * (size_t)(q0 + k * 256));
+#pragma unroll
+    for (uint32_t k = 0; k < kRangeBatch; ++k) {
+        if (k >= cnt || q0 + k * 256 >= n4) continue;
+        mn = fmin_nan(fmin_nan(mn, v[k].x), fmin_nan(v[k].y, fmin_nan(v[k].z, v[k].w)));
+        mx = fmax_nan(fmax_nan(mx, v[k].x), fmax_nan(v[k].y, fmax_nan(v[k].z, v[k].w)));
+    }
+    if ((uint64_t)(i + cnt) * kRangeItemElems >= n && tid < n - 4 * n4) {
+        const float x = in[4 * n4 + tid];
+        mn = fminf(mn, x), mx = fmaxf(mx, x);
+        nonfinite |= !isfinite(x);
     }
 }
 
@@ -1354,15 +1366,43 @@ __device__ __forceinline__ void compact_item(const FieldJob& J, uint32_t i)
 // kList false: one field, `one` (a kernel parameter: its fields are constant-bank operands
 // and take no registers); true: the fields jobs[] of a batch, located through segs[].
 template <bool kList>
-__global__ void __launch_bounds__(256) k_range_fields(const FieldJob* __restrict__ jobs, const Segment* __restrict__ segs,
+__global__ void __launch_bounds__(256, FZ_RANGE_CTAS) k_range_fields(const FieldJob* __restrict__ jobs, const Segment* __restrict__ segs,
                                                       uint32_t nseg, uint32_t total, const __grid_constant__ FieldJob one)
 {
     __shared__ uint32_t s_red[3][kCompressWarps];
-    for (uint32_t k = blockIdx.x; k < total; k += gridDim.x) {
-        uint32_t f = 0, i = k;
-        if (kList) locate(segs, nseg, k, f, i);
-        range_item(kList ? jobs[f] : one, i, s_red);
-        __syncthreads();  // s_red before the next item
+    uint32_t       k  = (uint32_t)((uint64_t)blockIdx.x * total / gridDim.x);
+    const uint32_t k1 = (uint32_t)((uint64_t)(blockIdx.x + 1) * total / gridDim.x);
+    if (k >= k1) return;  // (CTA-uniform)
+    // segment s (field f, items [fs, fend) of the launch) holds the run's first item
+    uint32_t s = 0, f = 0, fs = 0, fend = total;
+    if (kList) {
+        uint32_t hi = nseg - 1;
+        while (s < hi) {
+            const uint32_t mid = (s + hi + 1) >> 1;
+            if (__ldg(&segs[mid].start) <= k) s = mid;
+            else hi = mid - 1;
+        }
+        f    = __ldg(&segs[s].field);
+        fs   = __ldg(&segs[s].start);
+        fend = fs + __ldg(&segs[s].count);
+    }
+    for (;;) {
+        const FieldJob& J = kList ? jobs[f] : one;
+        const uint32_t  e = min(k1, fend);
+        float           mn = INFINITY, mx = -INFINITY;
+        uint32_t        nonfinite = 0;
+#pragma unroll 1
+        while (k < e) {  // ends with k == e: the next field's items start there
+            const uint32_t cnt = min(kRangeBatch, e - k);
+            range_items(J, k - fs, cnt, mn, mx, nonfinite);
+            k += cnt;
+        }
+        range_flush(J, mn, mx, nonfinite, s_red);
+        if (!kList || k >= k1) break;
+        ++s;  // the run goes on in the next field
+        f    = __ldg(&segs[s].field);
+        fs   = __ldg(&segs[s].start);
+        fend = fs + __ldg(&segs[s].count);
     }
 }
 
@@ -1373,7 +1413,7 @@ __global__ void __launch_bounds__(256) k_range_fields(const FieldJob* __restrict
 template <int ND>
 __host__ __device__ constexpr int encode_ring() { return ND == 1 ? kEncodeRing : 0; }
 template <int ND>
-__host__ __device__ constexpr int encode_ctas() { return ND == 3 ? 4 : (ND == 1 && kEncodeRing ? kEncodeCtas : 5); }
+__host__ __device__ constexpr int encode_ctas() { return ND == 3 ? 4 : (ND == 1 && kEncodeRing ? kEncodeCtas : FZ_ENCODE_CTAS_2D); }
 // Dynamic shared memory of an encode CTA: per warp the code image and the ring.
 template <int ND>
 __host__ __device__ constexpr uint32_t encode_smem() { return kCompressWarps * (kBlockWords * 4 + 1024u * encode_ring<ND>()); }

@@ -55,8 +55,8 @@ struct CompressArgs {
 
 // ------------------------------------------------------ list compression --
 // Compression of a list of fields in three launches (range, encode per dimensionality,
-// compaction), each a persistent grid striding over the list's items: range items (a
-// 16384-element chunk's max/min, relative eb only), encode items (8 shuffle blocks:
+// compaction), each a persistent grid over the list's items: range items (max/min of 1024
+// elements, relative eb only; a CTA takes a contiguous run), encode items (8 shuffle blocks:
 // codes, bitshuffle, flags, chunks into per-block slots) and compaction items (32 blocks:
 // offsets, chunks to their final place; the warp holding the last block writes the
 // header).  One field is a list of one, passed as a kernel parameter.
