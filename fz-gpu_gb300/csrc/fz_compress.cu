@@ -872,15 +872,20 @@ constexpr int kCompressWarps = 8;
 
 // Stream header (struct fz_header, include/fz.h), written once the stream's chunk count is
 // known.  flags: FZ_FLAG_CODE_OVERFLOW (1) and FZ_FLAG_FAILED (2).
-__device__ void write_header(const CompressArgs& a, const EbInfo& e, uint32_t flags, uint32_t nnz)
+__device__ void write_header(const CompressArgs& a, const EbInfo& e, uint32_t flags, uint32_t nnz,
+                             uint4* mirror = nullptr)
 {
-    uint8_t* h = a.out;
-    *reinterpret_cast<uint4*>(h + 0)  = make_uint4(0x31475A46u, 1u | (a.mode << 16) | (a.ndim << 24), a.x, a.y);
-    *reinterpret_cast<uint4*>(h + 16) = make_uint4(a.z, flags, a.n, 0u);
     const unsigned long long eb = __double_as_longlong(e.eb_abs);
-    *reinterpret_cast<uint4*>(h + 32) = make_uint4((uint32_t)eb, (uint32_t)(eb >> 32), __float_as_uint(e.ebx2_r),
-                                                   __float_as_uint(e.ebx2));
-    *reinterpret_cast<uint4*>(h + 48) = make_uint4(nnz, 0u, __float_as_uint(e.range), a.sidecar_bytes);
+    const uint4 w[4] = {make_uint4(0x31475A46u, 1u | (a.mode << 16) | (a.ndim << 24), a.x, a.y),
+                        make_uint4(a.z, flags, a.n, 0u),
+                        make_uint4((uint32_t)eb, (uint32_t)(eb >> 32), __float_as_uint(e.ebx2_r), __float_as_uint(e.ebx2)),
+                        make_uint4(nnz, 0u, __float_as_uint(e.range), a.sidecar_bytes)};
+    uint4* h = reinterpret_cast<uint4*>(a.out);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        h[k] = w[k];
+        if (mirror) mirror[k] = w[k];
+    }
 }
 
 
@@ -1271,30 +1276,41 @@ __device__ __forceinline__ void encode_item(const FieldJob& J, uint32_t i, float
     if (ovf && lane == 0) atomicOr(&J.ctl->flags, kCtlOverflow);
 }
 
-// The header of field J with `total` chunks, the offset table's total, and the control
-// words restored for the next call (one thread; after every encode item of the call).
-__device__ void finish_field(const FieldJob& J, uint32_t total)
+// The words the header of field J follows from, loaded by the thread that will write it as
+// early as they are final (the range and encode launches have finished), so that they
+// travel with its other loads.
+struct FieldFinal {
+    uint32_t mm0, mm1, flags, status, epoch;
+};
+__device__ __forceinline__ FieldFinal final_loads(const FieldJob& J)
+{
+    FieldFinal v;
+    v.mm0    = __ldcg(J.ctl->mm);
+    v.mm1    = __ldcg(J.ctl->mm + 1);
+    v.flags  = __ldcg(&J.ctl->flags);
+    v.epoch  = __ldcg(&J.ctl->epoch);
+    v.status = J.a.mirror ? __ldcg(J.a.status) : 0u;
+    return v;
+}
+
+// The header of field J with `total` chunks (and its copy in the mirror, with the status
+// word), the offset table's total, and the control words restored for the next call (one
+// thread; after every encode item of the call).
+__device__ void finish_field(const FieldJob& J, uint32_t total, const FieldFinal& v)
 {
     const CompressArgs& a  = J.a;
     FieldCtl*           C  = J.ctl;
-    const EbInfo        eb = J.rel ? eb_from_range(ord2f(__ldcg(C->mm)), ord2f(__ldcg(C->mm + 1)), a.eb_rel) : a.ebh;
-    const uint32_t      cf = __ldcg(&C->flags);
-    write_header(a, eb, ((cf & kCtlOverflow) ? 1u : 0u) | ((cf & kStatusNonfinite) ? 2u : 0u), total);
+    const EbInfo        eb = J.rel ? eb_from_range(ord2f(v.mm0), ord2f(v.mm1), a.eb_rel) : a.ebh;
+    // header and status in the mirror too, so a caller reads both with one copy
+    write_header(a, eb, ((v.flags & kCtlOverflow) ? 1u : 0u) | ((v.flags & kStatusNonfinite) ? 2u : 0u), total,
+                 reinterpret_cast<uint4*>(a.mirror));
+    if (a.mirror) a.mirror[16] = v.status;
     if (a.boff) {
         a.boff[a.nb] = total;  // the total closes the offset table; zero its 16-byte pad
         for (uint32_t k = a.nb + 1; k < (uint32_t)(pad16(4ull * (a.nb + 1)) / 4); ++k) a.boff[k] = 0;
     }
     C->mm[0] = 0xFFFFFFFFu, C->mm[1] = 0u;
     C->flags = 0;
-    if (a.mirror) {
-        // header and status in one place, so a caller reads both with one copy
-        __threadfence();
-        const uint4* h = reinterpret_cast<const uint4*>(a.out);
-        uint4*       m = reinterpret_cast<uint4*>(a.mirror);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) m[k] = __ldcg(h + k);
-        a.mirror[16] = __ldcg(a.status);
-    }
 }
 
 // Compaction item i of field J: blocks [32 i, 32 i + 32), four per warp, each warp on its
@@ -1305,7 +1321,7 @@ __device__ void finish_field(const FieldJob& J, uint32_t total)
 // prefix is <= q; 16-byte loads, four in flight per lane).  The call's group-sum set is
 // the parity bit of the counts; the warps clear the other set for the next call.  The warp
 // holding the last block knows the total: it writes the header and advances the call
-// counter.  No CTA reads what another compaction CTA writes: no barrier, fence or atomic.
+// counter.  No CTA uses what another compaction CTA writes: no barrier, fence or atomic.
 constexpr uint32_t kCompactWarpBlocks = kCompactBlocks / kCompressWarps;  // 4
 
 __device__ __forceinline__ void compact_item(const FieldJob& J, uint32_t i)
@@ -1314,21 +1330,30 @@ __device__ __forceinline__ void compact_item(const FieldJob& J, uint32_t i)
     const CompressArgs& a    = J.a;
     const uint32_t      gw = i * kCompressWarps + wid;  // warp of the launch's items of this field
     const uint32_t      b0 = gw * kCompactWarpBlocks, sup = b0 / kSuperBlocks;
-    // the call's set: the parity bit of any count of this call (block 0's); every warp of the
-    // field's items, past the last block too, clears its share of the other set
-    const uint32_t  par = __ldcg(J.counts) >> 31;
-    const uint32_t* set = J.supers + par * J.sstride;
-    uint32_t*       old = J.supers + (par ^ 1u) * J.sstride;
-    for (uint32_t k = gw * 32 + lane; k < J.sstride; k += J.nc * kCompressWarps * 32) old[k] = 0;
-    if (b0 >= a.nb) return;
+    const bool          live = b0 < a.nb, last = live && b0 + kCompactWarpBlocks >= a.nb;
+    // Every load the warp's offsets need is issued before any is used: the call's parity (the
+    // top bit of block 0's count), the group sums of both sets before the warp's group (the
+    // parity picks one), the counts before its blocks in its group and its own 4 counts; the
+    // last block's warp also loads the words its header follows from.
     static_assert(kSuperBlocks <= 64, "counts before a warp's blocks in its group: two per lane");
-    uint32_t acc = 0;
-    for (uint32_t k = lane; k < sup; k += 32) acc += __ldcg(set + k);
-    const uint32_t g0 = sup * kSuperBlocks;
-    if (g0 + lane < b0) acc += __ldcg(J.counts + g0 + lane) & ~kCountPar;
-    if (g0 + 32 + lane < b0) acc += __ldcg(J.counts + g0 + 32 + lane) & ~kCountPar;
-    const uint32_t c = lane < kCompactWarpBlocks && b0 + lane < a.nb ? __ldcg(J.counts + b0 + lane) & ~kCountPar : 0u;
-    const uint32_t exc = __reduce_add_sync(kFull, acc);
+    FieldFinal fin{};
+    if (last && lane == 0) fin = final_loads(J);
+    const uint32_t c0 = __ldcg(J.counts);
+    uint32_t       s0 = 0, s1 = 0, acc = 0, c = 0;
+    if (live) {
+        for (uint32_t k = lane; k < sup; k += 32) s0 += __ldcg(J.supers + k), s1 += __ldcg(J.supers + J.sstride + k);
+        const uint32_t g0 = sup * kSuperBlocks;
+        if (g0 + lane < b0) acc += __ldcg(J.counts + g0 + lane) & ~kCountPar;
+        if (g0 + 32 + lane < b0) acc += __ldcg(J.counts + g0 + 32 + lane) & ~kCountPar;
+        if (lane < kCompactWarpBlocks && b0 + lane < a.nb) c = __ldcg(J.counts + b0 + lane) & ~kCountPar;
+    }
+    // every warp of the field's items, past the last block too, clears its share of the set
+    // this call did not use (another warp may still read it above: that sum is discarded)
+    const uint32_t par = c0 >> 31;
+    uint32_t*      old = J.supers + (par ^ 1u) * J.sstride;
+    for (uint32_t k = gw * 32 + lane; k < J.sstride; k += J.nc * kCompressWarps * 32) old[k] = 0;
+    if (!live) return;
+    const uint32_t exc = __reduce_add_sync(kFull, acc + (par ? s1 : s0));
     // inclusive prefix of the 4 counts in lanes 0..3
     uint32_t v = c;
 #pragma unroll
@@ -1339,7 +1364,13 @@ __device__ __forceinline__ void compact_item(const FieldJob& J, uint32_t i)
     if (a.boff && lane < kCompactWarpBlocks && b0 + lane < a.nb) a.boff[b0 + lane] = exc + v - c;
     const uint32_t p1 = __shfl_sync(kFull, v - c, 1), p2 = __shfl_sync(kFull, v - c, 2);
     const uint32_t p3 = __shfl_sync(kFull, v - c, 3), tot = __shfl_sync(kFull, v, 3);
-    uint4*         B  = reinterpret_cast<uint4*>(a.out + a.off_b) + exc;
+    if (last && lane == 0) {
+        // the last block's warp: every count is in, so the total is exc + tot; the header
+        // needs none of the chunk moves below
+        finish_field(J, exc + tot, fin);
+        J.ctl->epoch = fin.epoch + 1u;  // the next call uses the set cleared here
+    }
+    uint4* B = reinterpret_cast<uint4*>(a.out + a.off_b) + exc;
     for (uint32_t q0 = lane; q0 < tot; q0 += 4 * 32) {
         uint4 val[4];
 #pragma unroll
@@ -1354,11 +1385,6 @@ __device__ __forceinline__ void compact_item(const FieldJob& J, uint32_t i)
 #pragma unroll
         for (int u = 0; u < 4; ++u)
             if (q0 + u * 32 < tot) B[q0 + u * 32] = val[u];
-    }
-    if (lane == 0 && b0 + kCompactWarpBlocks >= a.nb) {
-        // the last block's warp: every count is in, so the total is exc + tot
-        finish_field(J, exc + tot);
-        J.ctl->epoch += 1u;  // the next call uses the set cleared here
     }
 }
 
@@ -1449,10 +1475,7 @@ __global__ void __launch_bounds__(kCompressWarps * 32, encode_ctas<ND>())
         __syncthreads();  // the blocks' shared images before the next item
         // a field without full shuffle blocks has one encode item and no compaction: the
         // header is written here (its counter stays, no group sums were used)
-        if (J.a.nb == 0 && threadIdx.x == 0) {
-            __threadfence();
-            finish_field(J, 0u);
-        }
+        if (J.a.nb == 0 && threadIdx.x == 0) finish_field(J, 0u, final_loads(J));
     }
 }
 
