@@ -1,10 +1,9 @@
 // fz_noalloc.cu -- compression for callers that cannot allocate device memory.
 //
 // fz_compress needs a workspace, and creating one calls cudaMalloc.  Some callers cannot
-// do that: code that runs while a stream is being captured into a CUDA graph (an
-// allocation there breaks the capture), host frameworks that own every byte of device
-// memory through their own pool and forbid raw cudaMalloc, and latency-critical loops
-// where cudaMalloc's implicit synchronisation is unacceptable.  fz_compress_noalloc
+// do that: host frameworks that own every byte of device memory through their own pool
+// and forbid raw cudaMalloc, and latency-critical loops where cudaMalloc's implicit
+// synchronisation is unacceptable.  fz_compress_noalloc
 // serves them: the little scratch the scan needs lives in a fixed static device array in
 // this file, which every GPU that loads the library holds until the process exits.
 //

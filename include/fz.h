@@ -185,16 +185,14 @@ fz_status fz_decompress(fz_workspace* ws, const void* d_stream, uint64_t stream_
                         const fz_header* h_header, float* d_out, uint64_t out_capacity_elems,
                         fz_stream_t stream);
 
-/* Compression that allocates nothing, for callers that cannot call cudaMalloc: code
-   running while a stream is captured into a CUDA graph (an allocation would break the
-   capture), frameworks that own all device memory through their own pool, and loops
-   that cannot afford cudaMalloc's implicit synchronisation.  Same arguments and result
-   as fz_compress, without a workspace.  Its scratch is a fixed static device array of
+/* Compression that allocates nothing, for callers that cannot call cudaMalloc:
+   frameworks that own all device memory through their own pool, and loops that cannot
+   afford cudaMalloc's implicit synchronisation.  Same arguments and result as
+   fz_compress, without a workspace.  Its scratch is a fixed static device array of
    FZ_NOALLOC_SCRATCH_BYTES inside the library, held by every GPU that loads it until the
    process exits; fields larger than FZ_NOALLOC_MAX_ELEMS elements are rejected with
    FZ_INVALID_ARG before anything is launched.  The first call on a device looks up the
-   array's device address (cudaGetSymbolAddress), so make that first call before any
-   stream capture.  All calls share the array: calls whose GPU work overlaps race, so
+   array's device address (cudaGetSymbolAddress).  All calls share the array: calls whose GPU work overlaps race, so
    serialise them (one stream).  out_bytes (host, nullable) reads the size back and
    synchronises the stream; with it NULL the call returns without waiting, and a failure
    found on the device (NaN/Inf in a relative-eb input, a wait that gave up) marks the

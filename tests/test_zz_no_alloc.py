@@ -1,6 +1,6 @@
 """fz_compress_noalloc: compression for callers that cannot allocate device memory (for
-example code running while a stream is captured into a CUDA graph, or a framework that
-owns all device memory through its own pool).  Its scratch is a fixed static array inside
+example a framework that owns all device memory through its own pool).  Its scratch is a
+fixed static array inside
 the library.  This file is collected last so that a failure here comes after every other
 test has run; it also passes alone in a fresh process (the first call does the per-device
 set-up)."""
