@@ -223,7 +223,7 @@ fz_status fz_workspace_bytes(uint64_t max_n, uint64_t* bytes)
     b += 16;                        // range accumulators
     b += pad16(2 * max_n + 16);     // per-block slots (k_encode)
     b += pad16(4 * tiles + 4);      // block offsets
-    b += pad16(4 * 2 * (tiles / kSuperBlocks + 2));  // two sets of chunk counts per group of blocks
+    b += pad16(4 * 2 * (uint64_t)group_sum_words((uint32_t)tiles));  // two sets of group sums
     *bytes = b;
     return FZ_SUCCESS;
 }
@@ -253,8 +253,6 @@ fz_status fz_workspace_create(uint64_t max_n, fz_workspace** out)
     ws->status  = ws->tickets + 4;
     ws->total   = ws->tickets + 5;
     ws->epoch   = ws->tickets + 6;
-    ws->ovfw    = ws->tickets + 7;
-    ws->done    = ws->tickets + 8;
     ws->fctl    = reinterpret_cast<FieldCtl*>(ws->tickets + 16);
     p += 128;
     ws->mm       = reinterpret_cast<uint32_t*>(p), p += 16;
@@ -419,7 +417,8 @@ fz_status fz::compress_impl(fz_workspace* ws, const float* d_in, uint64_t n, fz_
     J.slots  = reinterpret_cast<uint4*>(ws->codes);
     J.counts = ws->boff;
     J.supers = ws->supers;
-    J.sstride = ws->max_tiles / kSuperBlocks + 2;
+    J.sstride = group_sum_words(ws->max_tiles);
+    J.s2off   = group_sum_l2(ws->max_tiles);
     J.rel    = eb_mode == FZ_EB_REL;
     field_items(L.n, L.nb, a.ntiles, J.rel != 0, J.nr, J.ne, J.nc);
     cudaError_t e = cudaSuccess;
@@ -701,7 +700,7 @@ fz_status plan_list_compress(fz_workspace* ws, const fz_field* f, uint32_t count
     std::vector<uint64_t> off(count);
     for (uint32_t i = 0; i < count; ++i) {
         off[i] = b_scr;
-        b_scr += 4096ull * lay[i].nb + pad16(4ull * (lay[i].nb + 2)) + pad16(8ull * (lay[i].nb / kSuperBlocks + 2));
+        b_scr += 4096ull * lay[i].nb + pad16(4ull * (lay[i].nb + 2)) + pad16(8ull * group_sum_words(lay[i].nb));
         b_scr = (b_scr + 255) & ~255ull;
     }
     uint8_t*    base = nullptr;
@@ -721,7 +720,8 @@ fz_status plan_list_compress(fz_workspace* ws, const fz_field* f, uint32_t count
         J.slots       = reinterpret_cast<uint4*>(scr + off[i]);
         J.counts      = reinterpret_cast<uint32_t*>(scr + off[i] + 4096ull * lay[i].nb);
         J.supers      = reinterpret_cast<uint32_t*>(scr + off[i] + 4096ull * lay[i].nb + pad16(4ull * (lay[i].nb + 2)));
-        J.sstride     = lay[i].nb / kSuperBlocks + 2;
+        J.sstride     = group_sum_words(lay[i].nb);
+        J.s2off       = group_sum_l2(lay[i].nb);
     }
     for (int k = 0; k < 5; ++k) {
         P.seg[k] = segd + hseg.size();

@@ -1270,7 +1270,11 @@ __device__ __forceinline__ void encode_item(const FieldJob& J, uint32_t i, float
         }
         if (lane == 0) {
             J.counts[t] = cnt | (par ? kCountPar : 0u);
-            if (cnt) atomicAdd(J.supers + par * J.sstride + t / kSuperBlocks, cnt);
+            if (cnt) {  // into the block's group sum of each level
+                uint32_t* set = J.supers + par * J.sstride;
+                atomicAdd(set + t / kSuperBlocks, cnt);
+                atomicAdd(set + J.s2off + t / kSuper2Blocks, cnt);
+            }
         }
     }
     if (ovf && lane == 0) atomicOr(&J.ctl->flags, kCtlOverflow);
@@ -1314,8 +1318,9 @@ __device__ void finish_field(const FieldJob& J, uint32_t total, const FieldFinal
 }
 
 // Compaction item i of field J: blocks [32 i, 32 i + 32), four per warp, each warp on its
-// own.  A warp's first chunk offset is the sum of this call's group sums (kSuperBlocks
-// blocks each) before its group plus the counts of the blocks of its group before its own;
+// own.  A warp's first chunk offset is the sum of this call's group sums before its group
+// (second-level sums of kSuper2Blocks blocks, then first-level sums of kSuperBlocks) plus
+// the counts of the blocks of its group before its own;
 // then it writes the offset table entries of its 4 blocks and moves their chunks from the
 // slots to Section B (output chunk q of the warp comes from the last of its blocks whose
 // prefix is <= q; 16-byte loads, four in flight per lane).  The call's group-sum set is
@@ -1329,19 +1334,25 @@ __device__ __forceinline__ void compact_item(const FieldJob& J, uint32_t i)
     const uint32_t      lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     const CompressArgs& a    = J.a;
     const uint32_t      gw = i * kCompressWarps + wid;  // warp of the launch's items of this field
-    const uint32_t      b0 = gw * kCompactWarpBlocks, sup = b0 / kSuperBlocks;
+    const uint32_t      b0 = gw * kCompactWarpBlocks, sup = b0 / kSuperBlocks, sup2 = b0 / kSuper2Blocks;
     const bool          live = b0 < a.nb, last = live && b0 + kCompactWarpBlocks >= a.nb;
     // Every load the warp's offsets need is issued before any is used: the call's parity (the
-    // top bit of block 0's count), the group sums of both sets before the warp's group (the
-    // parity picks one), the counts before its blocks in its group and its own 4 counts; the
-    // last block's warp also loads the words its header follows from.
-    static_assert(kSuperBlocks <= 64, "counts before a warp's blocks in its group: two per lane");
+    // top bit of block 0's count); in both sets (the parity picks one) the second-level sums
+    // before the warp's second-level group and the first-level sums before its first-level
+    // group inside it; the counts before its blocks in its first-level group and its own 4
+    // counts.  The last block's warp also loads the words its header follows from.
+    static_assert(kSuperBlocks <= 64 && kSuper2Blocks / kSuperBlocks <= 64, "inside a group: two loads per lane");
     FieldFinal fin{};
     if (last && lane == 0) fin = final_loads(J);
     const uint32_t c0 = __ldcg(J.counts);
     uint32_t       s0 = 0, s1 = 0, acc = 0, c = 0;
     if (live) {
-        for (uint32_t k = lane; k < sup; k += 32) s0 += __ldcg(J.supers + k), s1 += __ldcg(J.supers + J.sstride + k);
+        const uint32_t* L2 = J.supers + J.s2off;
+        for (uint32_t k = lane; k < sup2; k += 32) s0 += __ldcg(L2 + k), s1 += __ldcg(L2 + J.sstride + k);
+        const uint32_t h0 = sup2 * (kSuper2Blocks / kSuperBlocks);  // first-level groups before
+#pragma unroll
+        for (uint32_t k = lane; k < 64; k += 32)
+            if (h0 + k < sup) s0 += __ldcg(J.supers + h0 + k), s1 += __ldcg(J.supers + J.sstride + h0 + k);
         const uint32_t g0 = sup * kSuperBlocks;
         if (g0 + lane < b0) acc += __ldcg(J.counts + g0 + lane) & ~kCountPar;
         if (g0 + 32 + lane < b0) acc += __ldcg(J.counts + g0 + 32 + lane) & ~kCountPar;

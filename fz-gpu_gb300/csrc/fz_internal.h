@@ -76,9 +76,11 @@ struct FieldJob {
     FieldCtl*    ctl;
     uint4*       slots;   // 4 KiB per shuffle block
     uint32_t*    counts;  // chunks per block
-    uint32_t*    supers;  // two sets of `sstride` words: chunks per group of kSuperBlocks
-                          // blocks; a call adds into one set and clears the other
-    uint32_t     sstride;     // words per set (at least the field's groups)
+    uint32_t*    supers;  // two sets of `sstride` words of chunk counts: per group of
+                          // kSuperBlocks blocks, then (from word s2off) per group of
+                          // kSuper2Blocks; a call adds into one set and clears the other
+    uint32_t     sstride;     // words per set (group_sum_words)
+    uint32_t     s2off;       // first word of the second-level sums in a set
     uint32_t     nr, ne, nc;  // range, encode, compaction items
     uint32_t     rel;         // relative eb: the eb follows from the range items
 };
@@ -91,9 +93,15 @@ struct Segment {
 
 enum class FieldPhase { Range, Encode, Compact };
 
-// Shuffle blocks per group sum of chunk counts: a compaction warp's offset is the sum of
-// the group sums before its group plus at most 63 counts inside it -- one round of loads.
-constexpr uint32_t kSuperBlocks = 64;
+// Shuffle blocks per group sum of chunk counts, on two levels: a compaction warp's offset is
+// the second-level sums before its second-level group, plus at most 63 first-level sums
+// inside it, plus at most 63 counts inside its first-level group -- one round of loads
+// whose length grows with nb / 4096, not with nb.
+constexpr uint32_t kSuperBlocks  = 64;
+constexpr uint32_t kSuper2Blocks = kSuperBlocks * 64;
+// Words of one set of group sums for up to nb blocks, and where its second level starts.
+__host__ __device__ inline uint32_t group_sum_l2(uint32_t nb) { return nb / kSuperBlocks + 2; }
+__host__ __device__ inline uint32_t group_sum_words(uint32_t nb) { return group_sum_l2(nb) + nb / kSuper2Blocks + 2; }
 
 // Items of each kind for a field of n elements (ntiles scan tiles of shuffle blocks, nb full
 // blocks).

@@ -17,9 +17,7 @@ struct fz_workspace {
     uint32_t* status;
     uint32_t* total;
     uint32_t* epoch;    // device epoch of the scan state
-    uint32_t* ovfw;     // overflow bits of the two-launch compression (reset by k_compact)
-    uint32_t* done;     // k_compact CTAs finished (the last one resets it)
-    uint32_t* supers;   // chunk counts per 512 shuffle blocks
+    uint32_t* supers;   // two sets of group sums of chunk counts (FieldJob::supers)
     fz::FieldCtl* fctl; // control words of the list compression
     uint32_t* mm;       // range accumulators (min, max as ordered u32)
     uint16_t* codes;

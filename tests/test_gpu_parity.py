@@ -422,11 +422,12 @@ def test_batch_branch_counts_and_autotune(fz, oracle, synth):
 
 
 @pytest.mark.parametrize("nblocks,extra", [(512, 0), (1024, 0), (1025, 5), (31, 2047), (32, 0), (33, 1), (544, 100),
-                                           (64, 0), (65, 3), (127, 0), (128, 1), (4, 0), (5, 7)])
+                                           (64, 0), (65, 3), (127, 0), (128, 1), (4, 0), (5, 7),
+                                           (4095, 9), (4096, 0), (4097, 1), (8192, 2047), (8257, 0)])
 def test_compaction_group_boundaries(fz, oracle, ws, nblocks, extra):
-    """Fields ending exactly on or just past a 64-block count group, a 32-block compaction
-    item and a 4-block compaction warp: offsets, offset table and header match the
-    oracle."""
+    """Fields ending exactly on or just past a 64-block and a 4096-block count group, a
+    32-block compaction item and a 4-block compaction warp: offsets, offset table and
+    header match the oracle."""
     n = nblocks * 2048 + extra
     rng = np.random.default_rng(n)
     data = np.cumsum(rng.normal(0, 1, n)).astype(np.float32)
