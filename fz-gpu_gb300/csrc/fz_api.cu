@@ -221,7 +221,7 @@ fz_status fz_workspace_bytes(uint64_t max_n, uint64_t* bytes)
     b += pad16(8 * tiles);          // state
     b += 128;                       // tickets, status, total, field control words
     b += 16;                        // range accumulators
-    b += pad16(2 * max_n + 16);     // per-block slots (k_encode)
+    b += pad16(2 * max_n + 16);     // per-block slots (k_encode_fields)
     b += pad16(4 * tiles + 4);      // block offsets
     b += pad16(4 * 2 * (uint64_t)group_sum_words((uint32_t)tiles));  // two sets of group sums
     *bytes = b;

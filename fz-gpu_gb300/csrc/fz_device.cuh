@@ -118,6 +118,25 @@ __device__ __forceinline__ uint32_t pack_unsigned(float d)
 }
 
 // ------------------------------------------------------------- transpose --
+#ifndef FZ_TRANSPOSE_MUL
+#define FZ_TRANSPOSE_MUL 0
+#endif
+// x << J and x >> J as integer multiplies (the low and the high word of x * 2^J and of
+// x * 2^(32-J)), which run on the multiply-add pipe instead of the integer/logic one.
+template <int J>
+__device__ __forceinline__ uint32_t shl_mul(uint32_t x)
+{
+    uint32_t r;
+    asm("mul.lo.u32 %0, %1, %2;" : "=r"(r) : "r"(x), "n"(1u << J));
+    return r;
+}
+template <int J>
+__device__ __forceinline__ uint32_t shr_mul(uint32_t x)
+{
+    uint32_t r;
+    asm("mul.hi.u32 %0, %1, %2;" : "=r"(r) : "r"(x), "n"(1u << (32 - J)));
+    return r;
+}
 // 32x32 bit-matrix transpose in registers: bit c of a[r] becomes bit r of a[c].
 // Recursive off-diagonal block swap; the 16- and 8-bit stages are byte permutes.
 __device__ __forceinline__ void transpose32(uint32_t (&a)[32])
@@ -135,6 +154,16 @@ __device__ __forceinline__ void transpose32(uint32_t (&a)[32])
         a[r]        = __byte_perm(lo, hi, 0x6240);
         a[r + 8]    = __byte_perm(lo, hi, 0x7351);
     }
+#if FZ_TRANSPOSE_MUL
+#define FZ_SWAP_STAGE(J, M)                                        \
+    _Pragma("unroll") for (int r = 0; r < 32; ++r)                 \
+    {                                                              \
+        if (r & (J)) continue;                                     \
+        uint32_t lo = a[r], hi = a[r + (J)];                       \
+        a[r]        = (lo & (M)) | (shl_mul<(J)>(hi) & ~(M));      \
+        a[r + (J)]  = (hi & ~(M)) | (shr_mul<(J)>(lo) & (M));      \
+    }
+#else
 #define FZ_SWAP_STAGE(J, M)                                        \
     _Pragma("unroll") for (int r = 0; r < 32; ++r)                 \
     {                                                              \
@@ -143,6 +172,7 @@ __device__ __forceinline__ void transpose32(uint32_t (&a)[32])
         a[r]        = (lo & (M)) | ((hi << (J)) & ~(M));           \
         a[r + (J)]  = (hi & ~(M)) | ((lo >> (J)) & (M));           \
     }
+#endif
     FZ_SWAP_STAGE(4, 0x0F0F0F0Fu)
     FZ_SWAP_STAGE(2, 0x33333333u)
     FZ_SWAP_STAGE(1, 0x55555555u)
