@@ -131,15 +131,18 @@ __device__ __forceinline__ uint32_t sm_decode(uint32_t c)
     return (c & 0x8000u) ? 0u - mag : mag;
 }
 
-// Both sign-magnitude codes of a word w = c0 | c1 << 16 as two's-complement deltas.  An
-// arithmetic shift turns bit 15 (31) into an all-ones mask m, and (mag ^ m) - m is -mag
-// exactly when the sign is set -- sm_decode for both halves.
+// Both sign-magnitude codes of a word w = c0 | c1 << 16 as two's-complement deltas: the
+// sign bit 15 (31) spread into an all-ones mask m, (mag ^ m) - m is -mag exactly when the
+// sign is set -- sm_decode for both halves.
 __device__ __forceinline__ void sm_decode2(uint32_t w, uint32_t& d0, uint32_t& d1)
 {
-    const uint32_t m0 = static_cast<uint32_t>(static_cast<int32_t>(w << 16) >> 31);
-    const uint32_t m1 = static_cast<uint32_t>(static_cast<int32_t>(w) >> 31);
-    d0                = ((w & 0x7FFFu) ^ m0) - m0;
-    d1                = (((w >> 16) & 0x7FFFu) ^ m1) - m1;
+    // m0, m1: byte permutes whose selectors replicate the sign bit of byte 1 (bit 15) and of
+    // byte 3 (bit 31) into every byte (prmt's default mode, selector nibble 8 + byte)
+    uint32_t m0, m1;
+    asm("prmt.b32 %0, %1, 0, 0x9999;" : "=r"(m0) : "r"(w));
+    asm("prmt.b32 %0, %1, 0, 0xBBBB;" : "=r"(m1) : "r"(w));
+    d0 = ((w & 0x7FFFu) ^ m0) - m0;
+    d1 = ((__byte_perm(w, 0u, 0x4432) & 0x7FFFu) ^ m1) - m1;
 }
 
 // Decodes the 64 codes of group g (codes g*64 .. g*64+63) into 32 words w[j] =
@@ -183,7 +186,7 @@ __device__ __forceinline__ void decode_group(const DecodeArgs& a, uint32_t g, ui
             pw += __popc(bmi);
         }
         if (bad) atomicOr(a.status, kStatusCorrupt);
-        transpose32(w);  // w[p] = S[p*32 + gg]  ->  w[j] = W[gg*32 + j]
+        transpose32<true>(w);  // w[p] = S[p*32 + gg]  ->  w[j] = W[gg*32 + j]
     } else {
         const uint16_t* tc  = a.mode == 1 ? reinterpret_cast<const uint16_t*>(a.st + a.off_c) : nullptr;
         const uint32_t  e0  = g * 64;
@@ -537,7 +540,7 @@ __global__ void __launch_bounds__(kDecode1dWarps * 32) k_decompress1d(const Deco
         __syncwarp();
 #pragma unroll
         for (uint32_t p = 0; p < 32; ++p) w[p] = sm[p * 32 + lane];
-        transpose32(w);
+        transpose32<true>(w);
         __syncwarp();
     } else {
         decode_group(a, t * 32 + lane, w);  // tail: sidecar codes
