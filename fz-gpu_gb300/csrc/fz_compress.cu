@@ -33,6 +33,9 @@
 #ifndef FZ_ENCODE_CTAS
 #define FZ_ENCODE_CTAS 3
 #endif
+#ifndef FZ_BLOCK3D_UNROLL
+#define FZ_BLOCK3D_UNROLL 2
+#endif
 #ifndef FZ_ENCODE_CTAS_2D
 #define FZ_ENCODE_CTAS_2D 5
 #endif
@@ -41,6 +44,10 @@
 #endif
 
 namespace fz {
+
+// Group rows per iteration of block3d's loop: unrolled by 2 the rotation of the next row's
+// loads needs no register moves (hurricane-like 500x500x100 on GB300: 59.6 -> 57.8 us).
+constexpr int kBlock3dUnroll = FZ_BLOCK3D_UNROLL;
 
 __device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
@@ -626,7 +633,7 @@ __device__ __forceinline__ void block3d(const float* __restrict__ in, const Geo&
     }
     float          amax = 0.0f;  // max |d| (NaN if any d is NaN)
     const uint32_t prev = (lane + 31u) & 31u;
-#pragma unroll 1
+#pragma unroll kBlock3dUnroll
     for (uint32_t it = 0; it < 16; ++it) {
         uint32_t zn = zz, yn = yy, xn = xx;
         float4   vn = z4, unn = z4, ubn = z4, ucn = z4;
@@ -1320,10 +1327,10 @@ __device__ void finish_field(const FieldJob& J, uint32_t total, const FieldFinal
 // Compaction item i of field J: blocks [32 i, 32 i + 32), four per warp, each warp on its
 // own.  A warp's first chunk offset is the sum of this call's group sums before its group
 // (second-level sums of kSuper2Blocks blocks, then first-level sums of kSuperBlocks) plus
-// the counts of the blocks of its group before its own;
-// then it writes the offset table entries of its 4 blocks and moves their chunks from the
-// slots to Section B (output chunk q of the warp comes from the last of its blocks whose
-// prefix is <= q; 16-byte loads, four in flight per lane).  The call's group-sum set is
+// the counts of the blocks of its group before its own; then it writes the offset table
+// entries of its 4 blocks and moves their chunks from the slots to Section B (output chunk
+// q of the warp comes from the last of its blocks whose prefix is <= q; 16-byte loads,
+// four in flight per lane).  The call's group-sum set is
 // the parity bit of the counts; the warps clear the other set for the next call.  The warp
 // holding the last block knows the total: it writes the header and advances the call
 // counter.  No CTA uses what another compaction CTA writes: no barrier, fence or atomic.
