@@ -48,6 +48,10 @@ namespace fz {
 // Group rows per iteration of block3d's loop: unrolled by 2 the rotation of the next row's
 // loads needs no register moves (hurricane-like 500x500x100 on GB300: 59.6 -> 57.8 us).
 constexpr int kBlock3dUnroll = FZ_BLOCK3D_UNROLL;
+#ifndef FZ_BLOCK3D_U_UNROLL
+#define FZ_BLOCK3D_U_UNROLL 2
+#endif
+constexpr int kBlock3dUUnroll = FZ_BLOCK3D_U_UNROLL;  // the same for block3d_u (501x500x100: 84.0 -> 81.2 us)
 
 __device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
@@ -551,7 +555,7 @@ __device__ __forceinline__ void block3d_u(const float* __restrict__ in, const Ge
     float4         v    = ldg4(in + e0);
     float          amax = 0.0f;
     const uint32_t prev = (lane + 31u) & 31u;
-#pragma unroll 1
+#pragma unroll kBlock3dUUnroll
     for (uint32_t it = 0; it < 16; ++it) {
         const float4 vn   = it < 15 ? ldg4(in + e0 + 128) : v;
         const float  c[4] = {v.x, v.y, v.z, v.w};
