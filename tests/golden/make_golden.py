@@ -9,7 +9,10 @@ tests/golden/<case>.npz.  The exclusive scan between bitshuffle and encode is an
 integer prefix sum (cub::DeviceScan::ExclusiveSum, fz.cu:187-192); it is computed here
 with torch.cumsum on the device.
 
-    python tests/golden/make_golden.py [outdir]
+    python tests/golden/make_golden.py <outdir>
+
+The fixtures are written to <outdir> (then copied into tests/golden/ where the machine that
+ran them is not this one).
 """
 from __future__ import annotations
 
@@ -136,4 +139,6 @@ def run(outdir):
 
 
 if __name__ == "__main__":
-    run(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "golden"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <outdir>")
+    run(sys.argv[1])
