@@ -70,7 +70,8 @@ def test_compress_decompress_small(fz, oracle, synth, ws, kind, dims, eb, mode):
 # scalar ones), rows shorter and longer than a 2048-code block, 1D lengths around whole
 # blocks, and 3D rows and planes of few elements.
 WIDTHS = [((x, y, 1), 1e-3) for x, y in ((4, 1500), (8, 900), (12, 700), (124, 70), (128, 64), (132, 70),
-                                        (127, 66), (129, 65), (2044, 9), (2048, 8), (2052, 9), (4100, 5))]
+                                        (127, 66), (129, 65), (130, 66), (2044, 9), (2048, 8), (2049, 9),
+                                        (2050, 9), (2051, 9), (2052, 9), (4100, 5), (5, 900), (6, 800), (7, 700))]
 WIDTHS += [((n, 1, 1), 1e-3) for n in (2047, 2049, 4096, 6143, 10240 + 17)]
 WIDTHS += [((x, y, z), 1e-3) for x, y, z in ((4, 4, 300), (8, 9, 40), (128, 3, 12), (132, 5, 9), (127, 8, 8),
                                              (4, 513, 2))]
