@@ -308,13 +308,17 @@ __global__ void __launch_bounds__(256, 5) k_decompress2d(const DecodeArgs a, uin
     if (kAl) {
         const uint32_t nrows = min(16u, a.y - r0);
         uint32_t       lin0  = r0 * a.x + c0;  // first code of the window in row r0 + rr
+        // threads past the window's end read the row's first word (in bounds; their values
+        // only reach higher quad positions, which are past the end too, and are not stored)
+        const uint32_t t4 = live ? 4 * tid : 0u;
 #pragma unroll 4
         for (uint32_t rr = 0; rr < 16; ++rr) {
             if (rr >= nrows) break;  // uniform across the CTA
-            uint32_t d[4] = {0, 0, 0, 0};
-            if (live) {
-                const uint32_t i = (lin0 & 63u) + 4 * tid;
-                const uint2    v = *reinterpret_cast<const uint2*>(rows[rr] + (i >> 6) * kSlotWords + ((i & 63u) >> 1));
+            uint32_t d[4];
+            {
+                // code i of the row at word 36 (i >> 6) + (i & 63) / 2 = i / 2 + 4 (i >> 6)
+                const uint32_t i = (lin0 & 63u) + t4;
+                const uint2    v = *reinterpret_cast<const uint2*>(rows[rr] + (i >> 1) + 4 * (i >> 6));
                 sm_decode2(v.x, d[0], d[1]);
                 sm_decode2(v.y, d[2], d[3]);
             }
@@ -340,8 +344,10 @@ __global__ void __launch_bounds__(256, 5) k_decompress2d(const DecodeArgs a, uin
         const uint32_t row = r0 + rr;
         if (row >= a.y) break;  // uniform across the CTA
         const uint32_t lin0 = row * a.x + c0;
-        uint32_t       d[4] = {0, 0, 0, 0};
-        if (live) rb_read4<true>(rows[rr], (lin0 & 63u) + 4 * tid, d);
+        uint32_t       d[4];
+        // threads past the window's end read the row's first codes (same alignment, in bounds,
+        // never stored; their values reach only higher quad positions, past the end too)
+        rb_read4<true>(rows[rr], (lin0 & 63u) + (live ? 4 * tid : 0u), d);
         d[1] += d[0], d[2] += d[1], d[3] += d[2];
         uint32_t v = d[3];
         uint32_t u = __shfl_up_sync(kFull, v, 1);
