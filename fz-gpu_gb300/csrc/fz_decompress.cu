@@ -513,21 +513,28 @@ static cudaError_t allow_decompress3d_smem()
 // their sign; the others take it from the sidecar sign bits (or are non-negative).
 constexpr int kDecode1dWarps = 4;
 
-// Lane-local inclusive prefix of the lane's 64 deltas into shared memory (swizzled so the
-// 32 lanes hit 32 banks); codes at i%4 == 0 carry their sign, the others take it from the
-// sidecar words s0, s1.  kCheck: only the first lim deltas count (the run ends past x*y*z).
+// Word of prefix value j of lane l in a warp's shared buffer: the lane's 64 values as sixteen
+// 16-byte chunks, chunk c at position c ^ (l & 7), so that both the lanes' chunk stores here
+// and the output loop's chunk loads (16 lanes on one owner's 16 chunks) spread over all 32
+// banks.
+__device__ __forceinline__ uint32_t run1d_word(uint32_t l, uint32_t j) { return 64 * l + 4 * ((j >> 2) ^ (l & 7u)); }
+
+// Lane-local inclusive prefix of the lane's 64 deltas into shared memory, four values per
+// 16-byte store; codes at i%4 == 0 carry their sign, the others take it from the sidecar
+// words s0, s1.  kCheck: only the first lim deltas count (the run ends past x*y*z).
 template <bool kCheck>
 __device__ __forceinline__ uint32_t run1d(const uint32_t (&w)[32], uint32_t s0, uint32_t s1, uint32_t lim,
                                           uint32_t lane, uint32_t* sm)
 {
-    uint32_t acc = 0;
+    uint32_t acc = 0, q[4];
 #pragma unroll
     for (int j = 0; j < 64; ++j) {
         const uint32_t c   = (j & 1) ? (w[j >> 1] >> 16) : (w[j >> 1] & 0xFFFFu);
         const uint32_t sgn = ((j < 32 ? s0 >> j : s1 >> (j - 32)) & 1u);
         const uint32_t d   = (j & 3) == 0 ? sm_decode(c) : (sgn ? 0u - c : c);
         acc += (!kCheck || (uint32_t)j < lim) ? d : 0u;
-        sm[(j ^ lane) + 64 * lane] = acc;
+        q[j & 3] = acc;
+        if ((j & 3) == 3) *reinterpret_cast<uint4*>(sm + run1d_word(lane, j)) = make_uint4(q[0], q[1], q[2], q[3]);
     }
     return acc;
 }
@@ -574,12 +581,9 @@ __global__ void __launch_bounds__(kDecode1dWarps * 32) k_decompress1d(const Deco
         const uint32_t el = i * 128 + lane * 4;   // element within the block
         const uint32_t ow = el >> 6, j0 = el & 63u;  // owning lane, index in its run
         const uint32_t exo = __shfl_sync(kFull, ex, ow);
-        float          f[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t j = j0 + k;
-            f[k] = (float)(int32_t)(sm[(j ^ ow) + 64 * ow] + exo) * a.ebx2;
-        }
+        const uint4    pv  = *reinterpret_cast<const uint4*>(sm + run1d_word(ow, j0));  // j0 % 4 == 0
+        const float    f[4] = {(float)(int32_t)(pv.x + exo) * a.ebx2, (float)(int32_t)(pv.y + exo) * a.ebx2,
+                               (float)(int32_t)(pv.z + exo) * a.ebx2, (float)(int32_t)(pv.w + exo) * a.ebx2};
         const uint32_t e = t * kBlockCodes + el;
         if (e + 3 < a.nl) {
             *reinterpret_cast<float4*>(out + el) = make_float4(f[0], f[1], f[2], f[3]);
