@@ -15,8 +15,12 @@ autotuner picks.  A step holds 128 x 60.8 MB = 7.8 GB of input, far larger than 
              fz_decompress_host (pinned host memory, H2D and D2H copies inside the region):
              compressing host threads hand their streams to decompressing ones, so input
              copies and output copies share the host link at all times
+  value_without_graphs  the same steps as one fz_compress_batch / fz_decompress_batch
+             call per direction on one stream (each field's encode launch also takes the
+             range of the next field), no graph
   roofline   the dominant kernel's algorithmic bytes per launch / its mean event-timed
-             launch duration, against the measured HBM copy bandwidth
+             launch duration (per-field calls: the kernels of the graph's branches),
+             against the measured HBM copy bandwidth
   per_dimensionality  compress / decompress GB/s and kernel fractions of the other
              single-field workloads (cesm-like 2D, hurricane-like 3D, unaligned rows, 1D)
   batch      the 512-field mixed batch: every schedule the autotuner tries against the
@@ -324,22 +328,42 @@ def run_fz(args, rank, world, local_rank):
     gp.close()
     check_recon(X, Y, headers)
 
-    # Timed region 2 (kernel durations): steps issued as one batch call per direction
-    # without graphs, every kernel launch bracketed by a pair of CUDA events on the
-    # launching stream (workspace timing).
+    # Timed region 2 (kernel durations): the kernels of region 1's branches -- per field a
+    # range, an encode, a compaction and a decompression launch -- issued by per-field
+    # calls without graphs (every compression, then every decompression), every launch
+    # bracketed by a pair of CUDA events on the launching stream (workspace timing).
+    def step_fields():
+        st = 0
+        for i in range(nf):
+            st |= L.fz_compress(ws.handle, C.c_void_p(X[i].data_ptr()), n, dims, EB, fz.EB_REL, fz.MODE_SIDECAR,
+                                C.c_void_p(S[i].data_ptr()), cap, None, sh)
+        for i in range(nf):
+            st |= L.fz_decompress(ws.handle, C.c_void_p(S[i].data_ptr()), sizes[i], C.byref(headers[i]),
+                                  C.c_void_p(Y[i].data_ptr()), n, sh)
+        if st:
+            raise fz.FzError("bench step", st)
+
     ksteps = max(1, min(args.steps, 2))
     ws.enable_timing(ksteps * nf * 5 + 16)
     torch.cuda.synchronize()
+    for _ in range(ksteps):
+        step_fields()
+    torch.cuda.synchronize()
+    kern = {k: ws.kernel_time(k) for k in fz.Workspace.KERNELS}
+    ws.enable_timing(0)
+    launches = args.steps * sum(c for c, _ in kern.values()) // ksteps  # region 1 launches the same kernels
+    # Timed region 3 (value_without_graphs): the same steps as one batch call per direction
+    # on one stream, without graphs (each field's encode launch also takes the next field's
+    # range there), CUDA events around the whole region only.
     s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
     s0.record(stream)
     for _ in range(ksteps):
         step()
     s1.record(stream)
     torch.cuda.synchronize()
     calls_ms = s0.elapsed_time(s1)
-    kern = {k: ws.kernel_time(k) for k in fz.Workspace.KERNELS}
-    ws.enable_timing(0)
-    launches = args.steps * sum(c for c, _ in kern.values()) // ksteps  # region 1 launches the same kernels
+    check_recon(X, Y, headers)
 
     bytes_step = nf * 2 * 4 * n
     value = bytes_step * args.steps * world / (ms / 1e3) / 1e9

@@ -264,6 +264,7 @@ fz_status fz_workspace_create(uint64_t max_n, fz_workspace** out)
         const uint32_t init[2] = {0xFFFFFFFFu, 0u};  // empty min/max
         e                      = cudaMemcpy(ws->mm, init, sizeof(init), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(ws->fctl->mm, init, sizeof(init), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(ws->fctl->pre, init, sizeof(init), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = cudaMallocHost((void**)&ws->h_pinned, 128);
     if (e != cudaSuccess) {
@@ -395,8 +396,9 @@ static fz_status compress_args(const float* d_in, uint64_t n, fz_dims dims, doub
 // written by the last kernel; the request loop reads both with one copy).
 fz_status fz::compress_impl(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims dims, double eb,
                             fz_eb_mode eb_mode, fz_mode mode, void* d_out, uint64_t out_capacity,
-                            uint64_t* out_bytes, fz_stream_t stream, uint32_t* mirror)
+                            uint64_t* out_bytes, fz_stream_t stream, uint32_t* mirror, RangeAhead* ra)
 {
+    if (ra) ra->done = false;
     if (!ws) return FZ_INVALID_ARG;
     if (n > ws->max_n) return FZ_INVALID_ARG;
     fz_status st = check_device(ws);
@@ -421,6 +423,20 @@ fz_status fz::compress_impl(fz_workspace* ws, const float* d_in, uint64_t n, fz_
     J.s2off   = group_sum_l2(ws->max_tiles);
     J.rel    = eb_mode == FZ_EB_REL;
     field_items(L.n, L.nb, a.ntiles, J.rel != 0, J.nr, J.ne, J.nc);
+    if (ra && ra->have && J.rel) J.nr = 0;  // the previous call's encode launch took the range
+    // range ahead: only when a compaction launch follows the encode launch (it moves the
+    // accumulated range into place once every encode CTA has finished)
+    if (ra && ra->next && J.rel && J.nc) {
+        const fz_field& f = *ra->next;
+        Layout          Ln;
+        CompressArgs    an;
+        if (f.n <= ws->max_n && compress_args(static_cast<const float*>(f.src), f.n, f.dims, f.eb, eb_mode, mode, f.dst,
+                                              f.dst_capacity, ws->status, Ln, an) == FZ_SUCCESS) {
+            uint32_t ne, nc;
+            field_items(Ln.n, Ln.nb, an.ntiles, true, J.ahead_nr, ne, nc);
+            J.ahead_in = an.in, J.ahead_n = an.n;
+        }
+    }
     cudaError_t e = cudaSuccess;
     if (J.nr) {
         KernelTimer t(ws, s, 0);
@@ -428,13 +444,14 @@ fz_status fz::compress_impl(fz_workspace* ws, const float* d_in, uint64_t n, fz_
     }
     if (e == cudaSuccess) {
         KernelTimer t(ws, s, 1);
-        e = launch_fields(FieldPhase::Encode, (int)L.ndim, nullptr, nullptr, 0, J.ne, J, s);
+        e = launch_fields(FieldPhase::Encode, (int)L.ndim, nullptr, nullptr, 0, J.ne, J, s, J.ahead_nr);
     }
     if (e == cudaSuccess) {
         KernelTimer t(ws, s, 5);
         e = launch_fields(FieldPhase::Compact, (int)L.ndim, nullptr, nullptr, 0, J.nc, J, s);
     }
     if (e != cudaSuccess) return map_err(e);
+    if (ra) ra->done = J.ahead_nr != 0;
     if (out_bytes) {
         fz_header h;
         st = readback(ws, d_out, s, &h);
@@ -643,11 +660,14 @@ fz_status fz_compress_batch(fz_workspace* ws, const fz_field* fields, uint32_t c
                             fz_mode mode, fz_stream_t stream)
 {
     if (!ws || (!fields && count)) return FZ_INVALID_ARG;
+    fz::RangeAhead ra;  // each field's encode launch takes the next field's range
     for (uint32_t i = 0; i < count; ++i) {
         const fz_field& f = fields[i];
-        fz_status st = fz_compress(ws, static_cast<const float*>(f.src), f.n, f.dims, f.eb, eb_mode, mode,
-                                   f.dst, f.dst_capacity, nullptr, stream);
+        ra.next           = i + 1 < count ? fields + i + 1 : nullptr;
+        fz_status st = fz::compress_impl(ws, static_cast<const float*>(f.src), f.n, f.dims, f.eb, eb_mode, mode, f.dst,
+                                         f.dst_capacity, nullptr, stream, nullptr, &ra);
         if (st != FZ_SUCCESS) return st;
+        ra.have = ra.done;
     }
     return FZ_SUCCESS;
 }
@@ -714,7 +734,7 @@ fz_status plan_list_compress(fz_workspace* ws, const fz_field* f, uint32_t count
     std::vector<FieldCtl> hctl(count);
     std::vector<Segment>  hseg;
     for (uint32_t i = 0; i < count; ++i) {
-        hctl[i].mm[0] = 0xFFFFFFFFu;  // empty range
+        hctl[i].mm[0] = hctl[i].pre[0] = 0xFFFFFFFFu;  // empty ranges
         FieldJob& J   = jobs[i];
         J.ctl         = ctl + i;
         J.slots       = reinterpret_cast<uint4*>(scr + off[i]);
@@ -828,10 +848,20 @@ static fz_status capture_batch(fz_workspace* ws, const fz_field* comp, const fz_
             // fork: per-field work on parallel branches
             cudaEventRecord(ev[0], cs[0]);
             for (uint32_t i = 1; i < branches; ++i) cudaStreamWaitEvent(cs[i], ev[0], 0);
+            // one branch: each field's encode launch takes the range of the next field (on
+            // parallel branches the range launches already overlap other branches' kernels,
+            // and taking them into the encode launches measured slower)
+            std::vector<fz::RangeAhead> ra(branches);
             for (uint32_t i = 0; i < count && st == FZ_SUCCESS; ++i) {
                 const uint32_t k = i % branches;
                 fz_stream_t    h = reinterpret_cast<fz_stream_t>(cs[k]);
-                if (comp && !plan.d_mem) st = fz_compress_batch(wss[k], comp + i, 1, eb_mode, mode, h);
+                if (comp && !plan.d_mem) {
+                    const fz_field& f = comp[i];
+                    ra[k].next        = branches == 1 && i + 1 < count ? comp + i + 1 : nullptr;
+                    st = fz::compress_impl(wss[k], static_cast<const float*>(f.src), f.n, f.dims, f.eb, eb_mode, mode,
+                                           f.dst, f.dst_capacity, nullptr, h, nullptr, &ra[k]);
+                    ra[k].have = ra[k].done;
+                }
                 if (dec && st == FZ_SUCCESS) st = fz_decompress_batch(wss[k], dec + i, 1, h);
             }
             // join

@@ -1198,8 +1198,10 @@ __device__ __forceinline__ void locate(const Segment* __restrict__ segs, uint32_
 // so runs differ by at most one item, and keeps kRangeBatch loads per thread in flight.  The
 // running max/min of a thread is carried across its items and folded into the field's
 // accumulators once per field the run touches.
-__device__ __forceinline__ void range_flush(const FieldJob& J, float mn, float mx, uint32_t nonfinite,
-                                            uint32_t (*sred)[kCompressWarps])
+// The CTA's running max/min go into mm[0..1] (and a non-finite element into *flags and
+// *status) of the field they belong to.
+__device__ __forceinline__ void range_flush(uint32_t* mm, uint32_t* flags, uint32_t* status, float mn, float mx,
+                                            uint32_t nonfinite, uint32_t (*sred)[kCompressWarps])
 {
     // NaN leaves both NaN; -Inf shows in the min, +Inf in the max (the start values +Inf /
     // -Inf of a thread without elements stay on the other side)
@@ -1218,21 +1220,21 @@ __device__ __forceinline__ void range_flush(const FieldJob& J, float mn, float m
         const uint32_t c = __reduce_max_sync(kFull, lane < kCompressWarps ? sred[1][lane] : 0u);
         const uint32_t f = __reduce_or_sync(kFull, lane < kCompressWarps ? sred[2][lane] : 0u);
         if (lane == 0) {
-            atomicMin(J.ctl->mm, a);
-            atomicMax(J.ctl->mm + 1, c);
-            if (f) atomicOr(J.a.status, kStatusNonfinite), atomicOr(&J.ctl->flags, kStatusNonfinite);
+            atomicMin(mm, a);
+            atomicMax(mm + 1, c);
+            if (f) atomicOr(status, kStatusNonfinite), atomicOr(flags, kStatusNonfinite);
         }
     }
     __syncthreads();  // sred before the next flush
 }
 
-// Items [i, i + cnt) of field J (cnt <= kRangeBatch) into the thread's running max/min; the
-// field's last item also takes the n mod 4 elements past its 16-byte loads.
-__device__ __forceinline__ void range_items(const FieldJob& J, uint32_t i, uint32_t cnt, float& mn, float& mx,
-                                            uint32_t& nonfinite)
+// Items [i, i + cnt) of the n-element field at in (cnt <= kRangeBatch) into the thread's
+// running max/min; the field's last item also takes the n mod 4 elements past its 16-byte
+// loads.
+__device__ __forceinline__ void range_items(const float* __restrict__ in, uint32_t n, uint32_t i, uint32_t cnt,
+                                            float& mn, float& mx, uint32_t& nonfinite)
 {
-    const float*   in = J.a.in;
-    const uint32_t n = J.a.n, n4 = n / 4, tid = threadIdx.x;
+    const uint32_t n4 = n / 4, tid = threadIdx.x;
     const uint32_t q0 = i * (kRangeItemElems / 4) + tid;
     float4         v[kRangeBatch];
 #pragma unroll
@@ -1295,7 +1297,7 @@ __device__ __forceinline__ void encode_item(const FieldJob& J, uint32_t i, float
 // early as they are final (the range and encode launches have finished), so that they
 // travel with its other loads.
 struct FieldFinal {
-    uint32_t mm0, mm1, flags, status, epoch;
+    uint32_t mm0, mm1, flags, status, epoch, pre0, pre1, pre_flags;
 };
 __device__ __forceinline__ FieldFinal final_loads(const FieldJob& J)
 {
@@ -1305,12 +1307,16 @@ __device__ __forceinline__ FieldFinal final_loads(const FieldJob& J)
     v.flags  = __ldcg(&J.ctl->flags);
     v.epoch  = __ldcg(&J.ctl->epoch);
     v.status = J.a.mirror ? __ldcg(J.a.status) : 0u;
+    v.pre0      = __ldcg(J.ctl->pre);
+    v.pre1      = __ldcg(J.ctl->pre + 1);
+    v.pre_flags = __ldcg(&J.ctl->pre_flags);
     return v;
 }
 
 // The header of field J with `total` chunks (and its copy in the mirror, with the status
-// word), the offset table's total, and the control words restored for the next call (one
-// thread; after every encode item of the call).
+// word), the offset table's total, and the control words set for the next call: its range
+// and non-finite flag from pre (the range ahead this call's encode launch accumulated, or
+// the empty range), pre reset (one thread; after every encode item of the call).
 __device__ void finish_field(const FieldJob& J, uint32_t total, const FieldFinal& v)
 {
     const CompressArgs& a  = J.a;
@@ -1324,8 +1330,10 @@ __device__ void finish_field(const FieldJob& J, uint32_t total, const FieldFinal
         a.boff[a.nb] = total;  // the total closes the offset table; zero its 16-byte pad
         for (uint32_t k = a.nb + 1; k < (uint32_t)(pad16(4ull * (a.nb + 1)) / 4); ++k) a.boff[k] = 0;
     }
-    C->mm[0] = 0xFFFFFFFFu, C->mm[1] = 0u;
-    C->flags = 0;
+    C->mm[0] = v.pre0, C->mm[1] = v.pre1;
+    C->flags = v.pre_flags;
+    C->pre[0] = 0xFFFFFFFFu, C->pre[1] = 0u;
+    C->pre_flags = 0;
 }
 
 // Compaction item i of field J: blocks [32 i, 32 i + 32), four per warp, each warp on its
@@ -1442,10 +1450,10 @@ __global__ void __launch_bounds__(256, FZ_RANGE_CTAS) k_range_fields(const Field
 #pragma unroll 1
         while (k < e) {  // ends with k == e: the next field's items start there
             const uint32_t cnt = min(kRangeBatch, e - k);
-            range_items(J, k - fs, cnt, mn, mx, nonfinite);
+            range_items(J.a.in, J.a.n, k - fs, cnt, mn, mx, nonfinite);
             k += cnt;
         }
-        range_flush(J, mn, mx, nonfinite, s_red);
+        range_flush(J.ctl->mm, &J.ctl->flags, J.a.status, mn, mx, nonfinite, s_red);
         if (!kList || k >= k1) break;
         ++s;  // the run goes on in the next field
         f    = __ldg(&segs[s].field);
@@ -1465,6 +1473,35 @@ __host__ __device__ constexpr int encode_ctas() { return ND == 3 ? 4 : (ND == 1 
 // Dynamic shared memory of an encode CTA: per warp the code image and the ring.
 template <int ND>
 __host__ __device__ constexpr uint32_t encode_smem() { return kCompressWarps * (kBlockWords * 4 + 1024u * encode_ring<ND>()); }
+
+// Range ahead of a single-field encode launch over `total` items: the CTAs that took one
+// item fewer than the others (all CTAs when the items divide evenly; the CTAs without an
+// item when the grid, sized for the ahead field, is larger than `total`) split the ahead
+// field's range items into contiguous runs, as the range launch would, while the others
+// still encode -- the memory-bound pass fills the launch's last, partial wave.
+__device__ __forceinline__ void range_ahead(const FieldJob& J, uint32_t total)
+{
+    __shared__ uint32_t s_red[3][kCompressWarps];
+    const uint32_t      G = gridDim.x, rem = total % G;
+    uint32_t            c = blockIdx.x, m = G;
+    if (rem) {
+        if (c < rem) return;  // CTA-uniform
+        c -= rem, m = G - rem;
+    }
+    const uint32_t T = J.ahead_nr;
+    uint32_t       k = (uint32_t)((uint64_t)c * T / m);
+    const uint32_t k1 = (uint32_t)((uint64_t)(c + 1) * T / m);
+    if (k >= k1) return;
+    float    mn = INFINITY, mx = -INFINITY;
+    uint32_t nonfinite = 0;
+#pragma unroll 1
+    while (k < k1) {
+        const uint32_t cnt = min(kRangeBatch, k1 - k);
+        range_items(J.ahead_in, J.ahead_n, k, cnt, mn, mx, nonfinite);
+        k += cnt;
+    }
+    range_flush(J.ctl->pre, &J.ctl->pre_flags, J.a.status, mn, mx, nonfinite, s_red);
+}
 
 template <int ND, bool kList>
 __global__ void __launch_bounds__(kCompressWarps * 32, encode_ctas<ND>())
@@ -1498,6 +1535,9 @@ __global__ void __launch_bounds__(kCompressWarps * 32, encode_ctas<ND>())
         // a field without full shuffle blocks has one encode item and no compaction: the
         // header is written here (its counter stays, no group sums were used)
         if (J.a.nb == 0 && threadIdx.x == 0) finish_field(J, 0u, final_loads(J));
+    }
+    if constexpr (!kList) {
+        if (one.ahead_nr) range_ahead(one, total);
     }
 }
 
@@ -1590,7 +1630,7 @@ static uint32_t list_wave(int which, bool list)
 }
 
 cudaError_t launch_fields(FieldPhase phase, int nd, const FieldJob* jobs, const Segment* segs, uint32_t nseg,
-                          uint32_t total, const FieldJob& one, cudaStream_t s)
+                          uint32_t total, const FieldJob& one, cudaStream_t s, uint32_t min_ctas)
 {
     if (!total) return cudaSuccess;
     const bool list = jobs != nullptr;
@@ -1598,7 +1638,7 @@ cudaError_t launch_fields(FieldPhase phase, int nd, const FieldJob* jobs, const 
     const int      which = phase == FieldPhase::Range ? 0 : phase == FieldPhase::Encode ? nd : 4;
     const uint32_t wave  = list_wave(which, list);
     if (!wave) return cudaErrorInvalidDevice;
-    const dim3 grid(std::min(total, wave)), block(kCompressWarps * 32);
+    const dim3 grid(std::min(std::max(total, min_ctas), wave)), block(kCompressWarps * 32);
     if (phase == FieldPhase::Range) {
         if (list) k_range_fields<true><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one);
         else k_range_fields<false><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one);

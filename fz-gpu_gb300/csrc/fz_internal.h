@@ -61,14 +61,18 @@ struct CompressArgs {
 // offsets, chunks to their final place; the warp holding the last block writes the
 // header).  One field is a list of one, passed as a kernel parameter.
 
-// Per-field control words (device, 32 bytes).  Between calls: mm = {0xFFFFFFFF, 0},
-// flags 0 -- restored by whoever writes the header -- and epoch = the number of calls
-// that had full shuffle blocks.
+// Per-field control words (device, 32 bytes).  Between calls: mm = pre = {0xFFFFFFFF, 0},
+// flags = pre_flags = 0, and epoch = the number of calls that had full shuffle blocks.
+// Whoever writes a call's header moves pre/pre_flags into mm/flags and resets pre: a
+// call's encode launch may accumulate the range of the next field compressed with the
+// same control words into pre (range ahead), which that field's encode then reads from mm.
 struct FieldCtl {
-    uint32_t mm[2];    // range accumulators (order-preserving u32)
-    uint32_t flags;    // this call: kStatusNonfinite, bit 8 code overflow
-    uint32_t epoch;    // a call uses group-sum set (epoch & 1) and clears the other
-    uint32_t pad[4];
+    uint32_t mm[2];      // range accumulators (order-preserving u32)
+    uint32_t flags;      // this call: kStatusNonfinite, bit 8 code overflow
+    uint32_t epoch;      // a call uses group-sum set (epoch & 1) and clears the other
+    uint32_t pre[2];     // the next call's range accumulators (range ahead)
+    uint32_t pre_flags;  // the next call's kStatusNonfinite
+    uint32_t pad;
 };
 
 struct FieldJob {
@@ -83,6 +87,11 @@ struct FieldJob {
     uint32_t     s2off;       // first word of the second-level sums in a set
     uint32_t     nr, ne, nc;  // range, encode, compaction items
     uint32_t     rel;         // relative eb: the eb follows from the range items
+    // range ahead (single-field encode launches only): the range of ahead_n elements at
+    // ahead_in, ahead_nr range items, into ctl->pre by the CTAs that took the fewest
+    // encode items; ahead_nr == 0: none
+    const float* ahead_in;
+    uint32_t     ahead_n, ahead_nr;
 };
 
 // Items [start, start + count) of a list launch belong to field `field` (its items 0 ..
@@ -107,9 +116,11 @@ __host__ __device__ inline uint32_t group_sum_words(uint32_t nb) { return group_
 // blocks).
 void field_items(uint32_t n, uint32_t nb, uint32_t ntiles, bool rel, uint32_t& nr, uint32_t& ne, uint32_t& nc);
 // One list launch of `phase` (encode: of dimensionality nd) over `total` items: jobs/segs
-// device arrays of a batch, or jobs == nullptr and `one` the only field.
+// device arrays of a batch, or jobs == nullptr and `one` the only field.  The grid is
+// max(total, min_ctas) CTAs, at most one resident wave (min_ctas: an encode launch with
+// range ahead spreads the ahead field's range items over CTAs without encode items).
 cudaError_t launch_fields(FieldPhase phase, int nd, const FieldJob* jobs, const Segment* segs, uint32_t nseg,
-                          uint32_t total, const FieldJob& one, cudaStream_t s);
+                          uint32_t total, const FieldJob& one, cudaStream_t s, uint32_t min_ctas = 0);
 
 struct DecodeArgs {
     const uint8_t*  st;

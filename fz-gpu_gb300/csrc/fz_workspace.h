@@ -35,9 +35,17 @@ struct fz_workspace {
 };
 
 namespace fz {
+// Range ahead between consecutive compressions on one workspace and stream (relative eb):
+// the call's encode launch also accumulates the range of `next`, which that field's call
+// then takes instead of running its own range launch.
+struct RangeAhead {
+    const fz_field* next = nullptr;  // in: the field compressed next on this workspace, or null
+    bool            have = false;    // in: this call's range was accumulated by the previous call
+    bool            done = false;    // out: the range of `next` was accumulated
+};
 // fz_compress with an optional device mirror (128 bytes, 16-byte aligned) that receives
 // the 64-byte header and, at word 16, the status word once the stream is complete.
 fz_status compress_impl(fz_workspace* ws, const float* d_in, uint64_t n, fz_dims dims, double eb,
                         fz_eb_mode eb_mode, fz_mode mode, void* d_out, uint64_t out_capacity,
-                        uint64_t* out_bytes, fz_stream_t stream, uint32_t* mirror);
+                        uint64_t* out_bytes, fz_stream_t stream, uint32_t* mirror, RangeAhead* ra = nullptr);
 }  // namespace fz

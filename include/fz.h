@@ -268,8 +268,11 @@ typedef struct fz_field {
 typedef enum fz_direction { FZ_COMPRESS = 0, FZ_DECOMPRESS = 1 } fz_direction;
 
 /* Enqueues the whole batch on `stream` in one call (fields in order, one workspace:
-   its capacity must cover the largest field).  No counterpart in the reference,
-   which handles one file per process (fz.cu:226-238). */
+   its capacity must cover the largest field).  With a relative bound, each field's
+   encode launch also reads the next field's input for its value range (that field
+   then runs no range launch of its own), so every input of the batch must be ready
+   when the call is enqueued.  No counterpart in the reference, which handles one file
+   per process (fz.cu:226-238). */
 fz_status fz_compress_batch(fz_workspace* ws, const fz_field* fields, uint32_t count,
                             fz_eb_mode eb_mode, fz_mode mode, fz_stream_t stream);
 fz_status fz_decompress_batch(fz_workspace* ws, const fz_field* fields, uint32_t count,

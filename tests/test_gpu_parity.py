@@ -391,6 +391,61 @@ def test_graph_batch_replays_are_exact(fz, oracle, synth):
     assert ws.status() == fz.SUCCESS
 
 
+def test_batch_range_ahead_edges(fz, oracle, synth):
+    """Range ahead (each compression's encode launch takes the range of the next field on
+    its stream): a field without full shuffle blocks (no compaction launch, so the field
+    after it runs its own range launch), a 1D field with a tail, and a NaN field between
+    clean ones -- the NaN marks only its own header FZ_FLAG_FAILED and reaches the workspace
+    status; every other stream matches the oracle.  On one stream (fz_compress_batch) and
+    on 1 and 2 graph branches (the NaN field on a branch with its own workspace), replayed
+    twice."""
+    nanf = synth.smooth3d(40, 30, 20, seed=32).copy()
+    nanf[5000] = np.nan
+    items = [
+        (synth.smooth2d(700, 300, seed=31), (700, 300, 1), 1e-3),
+        (synth.smooth1d(1000, seed=33), (1000, 1, 1), 1e-3),
+        (synth.smooth1d(50000, seed=34), (50000, 1, 1), 1e-2),
+        (nanf, (40, 30, 20), 1e-3),
+        (synth.smooth2d(64, 64, seed=35), (64, 64, 1), 1e-4),
+        (synth.smooth1d(2053, seed=36), (2053, 1, 1), 1e-3),
+        (synth.peaks2d(1001, 77, seed=37, npeaks=20), (1001, 77, 1), 1e-3),
+    ]
+    bad = 3
+    ws = fz.Workspace(max(d.size for d, _, _ in items))
+    xs, ss, ys, comp = _batch_buffers(fz, items)
+    wants = {i: oracle.compress(d, dims, eb) for i, (d, dims, eb) in enumerate(items) if i != bad}
+
+    def check(what, status=True):
+        for i, s in enumerate(ss):
+            h = fz.parse_header(s[:64].cpu().numpy())
+            if i == bad:
+                assert h.flags & fz.FLAG_FAILED, what
+            else:
+                assert not h.flags & fz.FLAG_FAILED, (what, i)
+                assert_same_stream(s[: wants[i].size].cpu().numpy(), wants[i])
+        if status:  # the NaN field ran on the caller's workspace
+            assert ws.status() == fz.NONFINITE_INPUT, what
+        assert ws.status() == fz.SUCCESS, what  # reading the status clears it
+
+    for s in ss:
+        s.fill_(0x5A)
+    fz.compress_batch(ws, comp)
+    torch.cuda.synchronize()
+    check("one stream")
+    for branches in (1, 2):
+        g = fz.Batch(ws, comp, fz.COMPRESS, branches=branches)
+        for rep in range(2):
+            for s in ss:
+                s.fill_(0x3C + rep)
+            g.launch()
+            torch.cuda.synchronize()
+            check(f"{branches} branches, replay {rep}", status=bad % branches == 0)
+        g.close()
+    # the workspace is clean for a single call afterwards
+    d, dims, eb = items[0]
+    assert_same_stream(fz.compress(xs[0], dims, eb, ws=ws).cpu().numpy(), wants[0])
+
+
 def test_batch_branch_counts_and_autotune(fz, oracle, synth):
     """Every branch count gives the same streams and reconstructions; the autotuner
     times the candidates on these fields and returns one of them."""
