@@ -55,6 +55,8 @@ FIELDS = {
     "cesm": ((3600, 1800, 1), 1e-3, "smooth2d", "cesm-like 3600x1800 f32 (smooth, ~30% zeros), relative eb 1e-3"),
     "hurricane": ((500, 500, 100), 1e-3, "smooth3d", "hurricane-like 500x500x100 f32 (smooth 3D, ~40% zeros), relative eb 1e-3"),
     "exafel_u": ((39201, 388, 1), 1e-3, "peaks2d", "exafel-like 39201x388 f32 (rows not a multiple of 4), relative eb 1e-3"),
+    "hurricane_u": ((501, 500, 100), 1e-3, "smooth3d",
+                    "hurricane-like 501x500x100 f32 (rows not a multiple of 4), relative eb 1e-3"),
     "oned": ((1 << 25, 1, 1), 1e-3, "smooth1d", "1D 2^25 f32 (smooth series with zero runs), relative eb 1e-3"),
 }
 DIMS, EB, KIND, WORKLOAD = FIELDS["exafel"]
@@ -475,6 +477,7 @@ OTHERS = [("cesm-like 3600x1800", "smooth2d", (3600, 1800, 1), 1e-3, 16),
           ("hurricane-like 500x500x100", "smooth3d", (500, 500, 100), 1e-3, 6),
           ("hurricane-like 500x500x100 eb 1e-2", "smooth3d", (500, 500, 100), 1e-2, 6),
           ("exafel-like 39201x388 (rows not a multiple of 4)", "peaks2d", (39201, 388, 1), 1e-3, 8),
+          ("hurricane-like 501x500x100 (rows not a multiple of 4)", "smooth3d", (501, 500, 100), 1e-3, 6),
           ("1D 2^25", "smooth1d", (1 << 25, 1, 1), 1e-3, 4)]
 
 
