@@ -1425,6 +1425,8 @@ template <bool kList>
 __global__ void __launch_bounds__(256, FZ_RANGE_CTAS) k_range_fields(const FieldJob* __restrict__ jobs, const Segment* __restrict__ segs,
                                                       uint32_t nseg, uint32_t total, const __grid_constant__ FieldJob one)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ uint32_t s_red[3][kCompressWarps];
     uint32_t       k  = (uint32_t)((uint64_t)blockIdx.x * total / gridDim.x);
     const uint32_t k1 = (uint32_t)((uint64_t)(blockIdx.x + 1) * total / gridDim.x);
@@ -1508,6 +1510,8 @@ __global__ void __launch_bounds__(kCompressWarps * 32, encode_ctas<ND>())
     k_encode_fields(const FieldJob* __restrict__ jobs, const Segment* __restrict__ segs, uint32_t nseg, uint32_t total,
                     const __grid_constant__ FieldJob one)
 {
+    pdl_wait();
+    pdl_trigger();
     // per warp: the block's 4 KiB code image, then (1D/2D) its ring of input rows
     extern __shared__ __align__(16) uint32_t esm[];
     constexpr int kR = encode_ring<ND>();
@@ -1545,6 +1549,8 @@ template <bool kList>
 __global__ void __launch_bounds__(256) k_compact_fields(const FieldJob* __restrict__ jobs, const Segment* __restrict__ segs,
                                                         uint32_t nseg, uint32_t total, const __grid_constant__ FieldJob one)
 {
+    pdl_wait();
+    pdl_trigger();
     for (uint32_t k = blockIdx.x; k < total; k += gridDim.x) {
         uint32_t f = 0, i = k;
         if (kList) locate(segs, nseg, k, f, i);
@@ -1639,26 +1645,28 @@ cudaError_t launch_fields(FieldPhase phase, int nd, const FieldJob* jobs, const 
     const uint32_t wave  = list_wave(which, list);
     if (!wave) return cudaErrorInvalidDevice;
     const dim3 grid(std::min(std::max(total, min_ctas), wave)), block(kCompressWarps * 32);
+    // eager launches with programmatic stream serialization: each kernel's CTAs may start
+    // as the previous kernel of the call (or of the previous call on the stream) retires
     if (phase == FieldPhase::Range) {
-        if (list) k_range_fields<true><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one);
-        else k_range_fields<false><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one);
-    } else if (phase == FieldPhase::Compact) {
-        if (list) k_compact_fields<true><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one);
-        else k_compact_fields<false><<<grid, block, 0, s>>>(jobs, segs, nseg, total, one);
-    } else if (list) {
+        if (list) return launch_pdl(k_range_fields<true>, grid, block, 0, s, jobs, segs, nseg, total, one);
+        return launch_pdl(k_range_fields<false>, grid, block, 0, s, jobs, segs, nseg, total, one);
+    }
+    if (phase == FieldPhase::Compact) {
+        if (list) return launch_pdl(k_compact_fields<true>, grid, block, 0, s, jobs, segs, nseg, total, one);
+        return launch_pdl(k_compact_fields<false>, grid, block, 0, s, jobs, segs, nseg, total, one);
+    }
+    if (list) {
         switch (nd) {
-        case 1: k_encode_fields<1, true><<<grid, block, encode_smem<1>(), s>>>(jobs, segs, nseg, total, one); break;
-        case 2: k_encode_fields<2, true><<<grid, block, encode_smem<2>(), s>>>(jobs, segs, nseg, total, one); break;
-        default: k_encode_fields<3, true><<<grid, block, encode_smem<3>(), s>>>(jobs, segs, nseg, total, one); break;
-        }
-    } else {
-        switch (nd) {
-        case 1: k_encode_fields<1, false><<<grid, block, encode_smem<1>(), s>>>(jobs, segs, nseg, total, one); break;
-        case 2: k_encode_fields<2, false><<<grid, block, encode_smem<2>(), s>>>(jobs, segs, nseg, total, one); break;
-        default: k_encode_fields<3, false><<<grid, block, encode_smem<3>(), s>>>(jobs, segs, nseg, total, one); break;
+        case 1: return launch_pdl(k_encode_fields<1, true>, grid, block, encode_smem<1>(), s, jobs, segs, nseg, total, one);
+        case 2: return launch_pdl(k_encode_fields<2, true>, grid, block, encode_smem<2>(), s, jobs, segs, nseg, total, one);
+        default: return launch_pdl(k_encode_fields<3, true>, grid, block, encode_smem<3>(), s, jobs, segs, nseg, total, one);
         }
     }
-    return cudaGetLastError();
+    switch (nd) {
+    case 1: return launch_pdl(k_encode_fields<1, false>, grid, block, encode_smem<1>(), s, jobs, segs, nseg, total, one);
+    case 2: return launch_pdl(k_encode_fields<2, false>, grid, block, encode_smem<2>(), s, jobs, segs, nseg, total, one);
+    default: return launch_pdl(k_encode_fields<3, false>, grid, block, encode_smem<3>(), s, jobs, segs, nseg, total, one);
+    }
 }
 
 // One resident wave of k_compress<ND> on the current device.  The 64 KiB of dynamic shared

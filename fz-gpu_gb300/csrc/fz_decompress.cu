@@ -283,6 +283,8 @@ constexpr uint32_t kW2 = 960;
 template <bool kAl>
 __global__ void __launch_bounds__(256, 5) k_decompress2d(const DecodeArgs a, uint32_t nwin)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ __align__(16) uint32_t rows[16][16 * kSlotWords];  // 16 rows x 16 slots of 64 codes
     const uint32_t tid = threadIdx.x;
     const uint32_t bx = blockIdx.x % nwin, by = blockIdx.x / nwin;
@@ -382,6 +384,8 @@ constexpr uint32_t kW3 = 960;
 
 __global__ void __launch_bounds__(256, 4) k_decompress3d(const DecodeArgs a, const Brick3 k)
 {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ __align__(16) uint32_t rb3[];
     const uint32_t tid = threadIdx.x;
     const uint32_t bx = blockIdx.x % k.nwin, rest = blockIdx.x / k.nwin;
@@ -541,6 +545,8 @@ __device__ __forceinline__ uint32_t run1d(const uint32_t (&w)[32], uint32_t s0, 
 
 __global__ void __launch_bounds__(kDecode1dWarps * 32) k_decompress1d(const DecodeArgs a)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ __align__(16) uint32_t smem[kDecode1dWarps][2048];
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     const uint32_t t    = blockIdx.x * kDecode1dWarps + wid;
@@ -601,9 +607,8 @@ cudaError_t launch_decompress_fused(const DecodeArgs& a, cudaStream_t s)
     if (nd == 2) {
         const uint32_t nwin = (uint32_t)cdiv(a.x, kW2);
         const uint32_t ctas = (uint32_t)(nwin * cdiv(a.y, 16));
-        if (a.x % 4 == 0) k_decompress2d<true><<<ctas, 256, 0, s>>>(a, nwin);
-        else k_decompress2d<false><<<ctas, 256, 0, s>>>(a, nwin);
-        return cudaGetLastError();
+        if (a.x % 4 == 0) return launch_pdl(k_decompress2d<true>, dim3(ctas), dim3(256), 0, s, a, nwin);
+        return launch_pdl(k_decompress2d<false>, dim3(ctas), dim3(256), 0, s, a, nwin);
     }
     if (nd == 3) {
         const cudaError_t e = allow_decompress3d_smem();
@@ -611,12 +616,11 @@ cudaError_t launch_decompress_fused(const DecodeArgs& a, cudaStream_t s)
         const Brick3   k    = brick3(a.x, a.y);
         if (brick3_smem(k) > kDecompress3dSmemMax) return cudaErrorInvalidConfiguration;
         const uint64_t ctas = (uint64_t)k.nwin * k.nbgrp * cdiv(a.z, 8);
-        k_decompress3d<<<(uint32_t)ctas, 256, brick3_smem(k), s>>>(a, k);
-        return cudaGetLastError();
+        return launch_pdl(k_decompress3d, dim3((uint32_t)ctas), dim3(256), brick3_smem(k), s, a, k);
     }
     const uint32_t ntiles = a.nb + (a.tail ? 1u : 0u);
-    k_decompress1d<<<(uint32_t)cdiv(ntiles, kDecode1dWarps), kDecode1dWarps * 32, 0, s>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(k_decompress1d, dim3((uint32_t)cdiv(ntiles, kDecode1dWarps)), dim3(kDecode1dWarps * 32), 0, s,
+                      a);
 }
 
 // ------------------------------------------------------------- recon --

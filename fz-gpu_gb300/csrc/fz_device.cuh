@@ -15,6 +15,17 @@ constexpr uint32_t kBlockWords  = 1024;  // u32 words per shuffle block (fz.cu:7
 constexpr uint32_t kChunks      = 256;   // 16-byte chunks per shuffle block
 constexpr uint32_t kHeaderBytes = 64;
 
+// ------------------------------------------------- dependent launches --
+// Outside graph capture the path's kernels are launched with programmatic stream
+// serialization (launch_pdl): a kernel's CTAs may be scheduled while the previous kernel on
+// the stream finishes, so
+// each calls pdl_wait() before its first memory access -- it returns once the grids it
+// depends on have completed and their writes are visible (at once for a launch without
+// the attribute) -- and pdl_trigger() to let the next launch's CTAs take SMs as its own
+// retire.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // ---------------------------------------------------------------- eb info --
 // Written by the range pass (relative eb) or by the host (absolute eb).
 struct EbInfo {
