@@ -446,6 +446,33 @@ def test_batch_range_ahead_edges(fz, oracle, synth):
     assert_same_stream(fz.compress(xs[0], dims, eb, ws=ws).cpu().numpy(), wants[0])
 
 
+def test_batch_range_ahead_stops_at_an_invalid_field(fz, oracle, synth):
+    """A field whose arguments are invalid (input not 16-byte aligned) is not read ahead:
+    fz_compress_batch compresses the fields before it exactly, then returns
+    FZ_INVALID_ARG for it, and the workspace serves the next call normally."""
+    d0 = synth.smooth2d(700, 300, seed=41)
+    d1 = synth.smooth1d(50000, seed=42)
+    ws = fz.Workspace(d0.size)
+    x0 = torch.from_numpy(d0).cuda()
+    x1 = torch.zeros(d1.size + 1, device="cuda")
+    x1[1:] = torch.from_numpy(d1).cuda()
+    caps = [fz.max_compressed_bytes(d0.size, (700, 300, 1)), fz.max_compressed_bytes(d1.size, (d1.size, 1, 1))]
+    ss = [torch.full((c,), 0x11, dtype=torch.uint8, device="cuda") for c in caps]
+    comp = fz.fields_array([
+        {"src": x0.data_ptr(), "dst": ss[0].data_ptr(), "n": d0.size, "dims": (700, 300, 1), "eb": 1e-3,
+         "dst_capacity": caps[0]},
+        {"src": x1[1:].data_ptr(), "dst": ss[1].data_ptr(), "n": d1.size, "dims": (d1.size, 1, 1), "eb": 1e-3,
+         "dst_capacity": caps[1]}])
+    with pytest.raises(fz.FzError) as e:
+        fz.compress_batch(ws, comp)
+    assert e.value.status == fz.INVALID_ARG
+    want = oracle.compress(d0, (700, 300, 1), 1e-3)
+    assert_same_stream(ss[0][: want.size].cpu().numpy(), want)
+    assert ws.status() == fz.SUCCESS
+    want1 = oracle.compress(d1, (d1.size, 1, 1), 1e-3)
+    assert_same_stream(fz.compress(x1[1:].clone(), (d1.size, 1, 1), 1e-3, ws=ws).cpu().numpy(), want1)
+
+
 def test_batch_branch_counts_and_autotune(fz, oracle, synth):
     """Every branch count gives the same streams and reconstructions; the autotuner
     times the candidates on these fields and returns one of them."""
