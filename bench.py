@@ -74,10 +74,14 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--quick", action="store_true", help="headline only: no per-dimensionality, batch or serving keys")
-    p.add_argument("--workload", choices=["exafel", "batch", "serving", "kernels"], default="exafel",
+    p.add_argument("--workload", choices=["exafel", "batch", "serving", "kernels", "listkernels"], default="exafel",
                    help="exafel: the headline line (single-field workload, see --field); batch: 512 mixed "
                         "1D/2D/3D fields batched vs per field; serving: a Poisson request trace; kernels: "
-                        "every kernel kind on the --field workload, --steps times (for a profiler)")
+                        "every kernel kind on the --field workload, --steps times (for a profiler); "
+                        "listkernels: the batch schedule's list launches on --list-fields fields of the mix, "
+                        "--steps times (for a profiler)")
+    p.add_argument("--list-fields", type=int, default=32,
+                   help="listkernels: the first fields of the 512-field mix of at most 32 MB")
     p.add_argument("--field", choices=sorted(FIELDS), default="exafel",
                    help="the single-field workload of the headline line (default exafel)")
     p.add_argument("--batch-fields", type=int, default=512)
@@ -860,6 +864,49 @@ def run_serving(args, local_rank):
     return out
 
 
+def run_list_kernels(args, local_rank):
+    """The list launches of a batch compression -- one range launch over every field, one
+    encode launch per dimensionality present, one compaction launch -- on the first
+    --list-fields fields of the 512-field mix of at most 32 MB (1D/2D/3D, rows that are and
+    are not a multiple of 4, every eb), --steps times, every stream checked against the
+    per-field calls' after the last step.  Prints one line naming a step's launches."""
+    import importlib
+    import numpy as np
+    import torch
+    import __graft_entry__ as g
+    fz = g.load_package()
+    synth = importlib.import_module("fz_gpu_gb300.synth")
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    specs = [sp for sp in synth.mixed_specs(512, seed=3) if 4 * int(np.prod(sp[1])) <= 32 << 20][:args.list_fields]
+    X = _torch_fields(specs, dev)
+    ns = [x.numel() for x in X]
+    caps = [fz.max_compressed_bytes(n, d) for n, (_, d, _, _) in zip(ns, specs)]
+    S = [torch.empty(c, dtype=torch.uint8, device=dev) for c in caps]
+    ws = fz.Workspace(max(ns))
+    ref = [fz.compress(x, d, eb, ws=ws).clone() for x, (_, d, eb, _) in zip(X, specs)]
+    comp = fz.fields_array([{"src": x.data_ptr(), "dst": s_.data_ptr(), "n": n, "dims": d, "eb": eb,
+                             "dst_capacity": s_.numel()} for x, s_, n, (_, d, eb, _) in zip(X, S, ns, specs)])
+    gb = fz.Batch.scheduled(ws, comp, None, fz.Schedule(1, 1))
+    for _ in range(args.steps):
+        gb.launch()
+    torch.cuda.synchronize()
+    gb.close()
+    assert all(torch.equal(s_[: r.numel()], r) for s_, r in zip(S, ref))
+    nds = sorted({fz.ndim(d) for _, d, _, _ in specs})
+    by_nd = {d: {"fields": 0, "elems": 0, "stream_bytes": 0} for d in nds}
+    for (_, d, _, _), n, r in zip(specs, ns, ref):
+        k = by_nd[fz.ndim(d)]
+        k["fields"] += 1
+        k["elems"] += n
+        k["stream_bytes"] += r.numel()
+    print(json.dumps({"workload": f"the first {len(specs)} fields of the 512-field mix of at most 32 MB "
+                                  f"({4 * sum(ns) / 1e6:.0f} MB, dimensionalities {nds})", "steps": args.steps,
+                      "per_step": ["k_range_fields<list>"] + [f"k_encode_fields<{d}, list>" for d in nds] +
+                                  ["k_compact_fields<list>"],
+                      "by_dimensionality": by_nd}))
+
+
 def run_kernels(args, local_rank):
     """Every kernel kind once per step on one --field field: compression (range, encode,
     compaction), decompression of the sidecar stream, decompression of a COMPAT stream
@@ -912,6 +959,9 @@ def main():
     elif args.workload == "kernels":
         if rank == 0:
             run_kernels(args, local_rank)
+    elif args.workload == "listkernels":
+        if rank == 0:
+            run_list_kernels(args, local_rank)
     else:
         run_fz(args, rank, world, local_rank)
 
