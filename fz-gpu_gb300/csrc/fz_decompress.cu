@@ -363,6 +363,99 @@ __global__ void __launch_bounds__(256, 5) k_decompress2d(const DecodeArgs a, uin
     }
 }
 
+// ------------------------------------------- fused 2D decode, x % 16 == 0 --
+// Rows a multiple of 16 elements long: every 16-column tile row lies inside one 64-code
+// group (group and tile boundaries are both multiples of 16 in the linear index), so
+// phase 1 does the whole x direction.  Thread (row rr, j) decodes group glo(rr) + j, and for
+// each of its four tiles inside the window decodes the 16 codes, prefix-sums them serially
+// and writes the 16 partial sums as 32-bit words into the window's row (chunk c of 4 words
+// at c ^ ((c >> 4) & 7): the lanes' stores, 64 words apart, and phase 2's loads spread over
+// all banks).  Phase 2: thread t owns columns 4t..4t+3 -- a running sum over the band's
+// rows, (float)p * ebx2, coalesced stores; no shuffles, so threads past the window leave.
+constexpr uint32_t kW16 = 960;
+constexpr uint32_t kX16Smem = 16 * kW16 * 4;  // 16 rows x 960 partial sums
+
+__device__ __forceinline__ uint32_t x16_chunk(uint32_t c) { return c ^ ((c >> 4) & 7u); }
+
+__global__ void __launch_bounds__(256, 3) k_decompress2d_x16(const DecodeArgs a, uint32_t nwin)
+{
+    pdl_wait();
+    pdl_trigger();
+    extern __shared__ __align__(16) uint32_t xs[];  // [16][kW16] partial sums along x
+    const uint32_t tid = threadIdx.x;
+    const uint32_t bx = blockIdx.x % nwin, by = blockIdx.x / nwin;
+    const uint32_t c0 = bx * kW16, c1 = min(c0 + kW16, a.x);
+    const uint32_t r0 = by * 16;
+    {
+        const uint32_t rr = tid >> 4, j = tid & 15u, row = r0 + rr;
+        if (row < a.y) {
+            const uint32_t lin0 = row * a.x + c0, lin1 = row * a.x + c1;
+            const uint32_t g = (lin0 >> 6) + j;
+            if (g <= ((lin1 - 1) >> 6)) {
+                uint32_t w[32];
+                decode_group(a, g, w);
+                uint32_t* xr = xs + rr * kW16;
+#pragma unroll
+                for (uint32_t q = 0; q < 4; ++q) {
+                    const uint32_t e = g * 64 + q * 16;  // the tile row's first code
+                    if (e < lin0 || e >= lin1) continue;
+                    uint32_t v[16], acc = 0;
+#pragma unroll
+                    for (uint32_t k = 0; k < 8; ++k) {
+                        uint32_t d0, d1;
+                        sm_decode2(w[8 * q + k], d0, d1);
+                        acc += d0, v[2 * k] = acc;
+                        acc += d1, v[2 * k + 1] = acc;
+                    }
+                    const uint32_t c = (e - lin0) >> 2;  // first chunk of the tile row in the window row
+#pragma unroll
+                    for (uint32_t s = 0; s < 4; ++s)
+                        *reinterpret_cast<uint4*>(xr + 4 * x16_chunk(c + s)) =
+                            make_uint4(v[4 * s], v[4 * s + 1], v[4 * s + 2], v[4 * s + 3]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t col = c0 + 4 * tid;
+    if (col >= c1) return;  // phase 2 has no shuffles or barriers
+    const uint32_t nrows = min(16u, a.y - r0);
+    const uint32_t* xp   = xs + 4 * x16_chunk(tid);
+    float*          out  = a.out + (size_t)r0 * a.x + col;
+    uint32_t        acc[4] = {0, 0, 0, 0};
+#pragma unroll 4
+    for (uint32_t rr = 0; rr < 16; ++rr) {
+        if (rr >= nrows) break;  // uniform across the CTA
+        const uint4 p = *reinterpret_cast<const uint4*>(xp + rr * kW16);
+        acc[0] += p.x, acc[1] += p.y, acc[2] += p.z, acc[3] += p.w;
+        *reinterpret_cast<float4*>(out) = make_float4((float)(int32_t)acc[0] * a.ebx2, (float)(int32_t)acc[1] * a.ebx2,
+                                                      (float)(int32_t)acc[2] * a.ebx2, (float)(int32_t)acc[3] * a.ebx2);
+        out += a.x;
+    }
+}
+
+// Resident CTAs of k_decompress2d_x16 on the current device (0 on error), cached per device;
+// the first call also opts the kernel in to its dynamic shared memory (above 48 KB).
+static uint32_t x16_wave()
+{
+    static std::atomic<uint32_t> cache[64];
+    int                          dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    std::atomic<uint32_t>* slot = (dev >= 0 && dev < 64) ? &cache[dev] : nullptr;
+    uint32_t               w    = slot ? slot->load(std::memory_order_acquire) : 0u;
+    if (w) return w;
+    int sms = 0, per_sm = 0;
+    if (cudaFuncSetAttribute(k_decompress2d_x16, cudaFuncAttributeMaxDynamicSharedMemorySize, kX16Smem) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_decompress2d_x16, 256, kX16Smem) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0;
+    }
+    w = (uint32_t)std::max(0, sms * per_sm);
+    if (slot && w) slot->store(w, std::memory_order_release);
+    return w;
+}
+
 // ------------------------------------------------------ fused 3D decode --
 // A CTA owns `bands` 8-row tile bands x one 8-plane tile slab x a window of w columns
 // (w a multiple of 8, at most 960); the flat block index runs over windows, then band
@@ -604,6 +697,16 @@ __global__ void __launch_bounds__(kDecode1dWarps * 32) k_decompress1d(const Deco
 cudaError_t launch_decompress_fused(const DecodeArgs& a, cudaStream_t s)
 {
     const int nd = (a.z == 1 && a.y == 1) ? 1 : (a.z == 1 ? 2 : 3);
+    if (nd == 2 && a.x % 16 == 0) {
+        // the x-in-phase-1 kernel (3 CTAs/SM) when its grid is one resident wave: measured on
+        // GB300, cesm-like 3600x1800 (452 CTAs) 14.0 -> 12.2 us a launch (in 8-branch graphs,
+        // where it leaves less room to other branches' kernels, the same throughput);
+        // exafel-like 39200x388 (1025 CTAs: 2.25 waves against 1.35 for k_decompress2d at 5
+        // CTAs/SM) 20.4 us either way
+        const uint32_t nwin = (uint32_t)cdiv(a.x, kW16);
+        const uint32_t ctas = (uint32_t)(nwin * cdiv(a.y, 16));
+        if (ctas <= x16_wave()) return launch_pdl(k_decompress2d_x16, dim3(ctas), dim3(256), kX16Smem, s, a, nwin);
+    }
     if (nd == 2) {
         const uint32_t nwin = (uint32_t)cdiv(a.x, kW2);
         const uint32_t ctas = (uint32_t)(nwin * cdiv(a.y, 16));
