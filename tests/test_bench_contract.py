@@ -33,3 +33,13 @@ def test_reference_arm_prints_one_contract_line():
 
 def test_reference_arm_other_ranks_print_nothing():
     assert _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []
+
+
+def test_product_arm_fails_loudly_without_a_gpu():
+    """The product arm has no CPU fallback: without a CUDA device it exits non-zero and
+    prints no benchmark line."""
+    r = subprocess.run([sys.executable, "bench.py", "--steps", "1", "--warmup", "0", "--quick", "--no-e2e"],
+                       cwd=ROOT, env=dict(os.environ, CUDA_VISIBLE_DEVICES=""), capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode != 0
+    assert not [l for l in r.stdout.splitlines() if l.startswith("{")]
