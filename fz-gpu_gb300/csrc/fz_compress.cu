@@ -1526,7 +1526,8 @@ __global__ void __launch_bounds__(kCompressWarps * 32, encode_ctas<ND>())
         if (kList) locate(segs, nseg, k, f, i);
         const FieldJob& J = kList ? jobs[f] : one;
         if (threadIdx.x == 0 && s_rf != f) {
-            // ebx2_r of the field: from its range (relative eb; the range launch has finished);
+            // ebx2_r of the field: from its range (relative eb; complete once the range launch,
+            // or the previous call's encode launch for a range ahead, has finished);
             // the call's group-sum set (the compaction launch moves the counter on)
             s_r   = J.rel ? eb_from_range(ord2f(__ldcg(J.ctl->mm)), ord2f(__ldcg(J.ctl->mm + 1)), J.a.eb_rel).ebx2_r
                           : J.a.ebh.ebx2_r;
